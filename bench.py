@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Jacobi backend on the square800 paste workload.
+
+Workload (one step): the fpie GridSolver path on the 'square800' problem --
+an 800x800 square (640,000 unknowns, 802x802 crop) pasted from a 900^2
+source into a 1024^2 target with the 'max' gradient -- reset from inputs
+already resident in HBM, then 5000 FP32 Jacobi sweeps, the residual and the
+uint8 image.  Metric: pixel-updates/s = unknowns x sweeps / time.
+
+Printed JSON line (rank 0):
+* ``value``     device-timed (CUDA events on the launching stream), inputs in
+                HBM; L2 is flushed between steps (a 512 MiB write), outside
+                the timed events;
+* ``e2e``       the same work through the plugin API a user calls:
+                ``GridSolver.reset`` from pinned host arrays (H2D inside) and
+                ``GridSolver.step(5000)`` returning the uint8 image (D2H);
+* ``roofline``  the sweep kernel: algorithmic bytes per launch / its average
+                launch duration, against the measured HBM copy bandwidth;
+* ``cpu_baseline`` the oracle's C restatement (OpenMP, all host threads) on a
+                bounded number of sweeps of the same problem;
+* ``equ``       the EquSolver form of the same problem, device-timed.
+
+``--impl reference`` times the CPU implementation of the path instead (the
+C restatement of the reference's Jacobi solvers, all host threads), on a
+bounded sample of each step, and prints the same metric.  Under torchrun
+with N>1 every rank runs an independent replica (the path has no exchange
+step); the reference arm runs on rank 0 only.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SWEEPS = 5000
+GRID_BYTES_PER_PX = 37   # read x 12 + read grad 12 + write x 12 + mask 1 (FP32 sweep)
+EQU_BYTES_PER_UNKNOWN = 52  # A 16 + B 12 + read X 12 + write X 12
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=40)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--sweeps", type=int, default=SWEEPS)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-equ", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic(name: str):
+    """dram bytes per launch from a committed ncu summary, if there is one."""
+    f = ROOT / "profiles" / f"{name}.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 100 ms) while the timed region runs."""
+
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={','.join(self.FIELDS)}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.flush()
+        rows = []
+        with open(self.out.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) == len(self.FIELDS):
+                    rows.append(parts)
+        os.unlink(self.out.name)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "", 1).isdigit()), default=None)}
+
+
+def square800_inputs():
+    from fpie_gb300 import prep, workloads
+
+    pb = workloads.square800(SWEEPS)
+    mc, t, g, _ = prep.grid_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, pb.gradient)
+    return pb, mc, t, g
+
+
+def cpu_baseline_grid(mc, t, g, budget_s: float = 10.0):
+    """The oracle's C restatement timed on a bounded number of sweeps."""
+    from oracle import cjacobi
+
+    th = host_threads()
+    o = cjacobi.CGrid(mc, t, g, nthreads=th)
+    o.sweep(3)
+    t0 = time.perf_counter()
+    o.sweep(20)
+    per = (time.perf_counter() - t0) / 20
+    n_sw = int(max(20, min(SWEEPS, budget_s / max(per, 1e-9))))
+    o = cjacobi.CGrid(mc, t, g, nthreads=th)
+    t0 = time.perf_counter()
+    o.sweep(n_sw)
+    o.err64()
+    o.image()
+    dt = time.perf_counter() - t0
+    unknowns = int((mc != 0).sum())
+    return {"value": unknowns * n_sw / dt, "unit": "pixel-updates/s", "cores": th, "kind": "port",
+            "sample": f"{n_sw} of {SWEEPS} sweeps of square800 GridSolver (640,000 unknowns) + residual + "
+                      f"clip, oracle C restatement (OpenMP), {th} threads, {dt:.2f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import cjacobi
+
+    pb, mc, t, g = square800_inputs()
+    unknowns = int((mc != 0).sum())
+    th = host_threads()
+    o = cjacobi.CGrid(mc, t, g, nthreads=th)
+    o.sweep(2)
+    t0 = time.perf_counter()
+    o.sweep(10)
+    per = (time.perf_counter() - t0) / 10
+    # Each step is a bounded sample so the whole run stays within ~2 minutes.
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    n_sw = int(max(10, min(args.sweeps, budget / max(per, 1e-9))))
+
+    def one_step():
+        s = cjacobi.CGrid(mc, t, g, nthreads=th)  # reset: copy the inputs
+        s.sweep(n_sw)
+        s.err64()
+        s.image()
+
+    for _ in range(args.warmup):
+        one_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    dt = time.perf_counter() - t0
+    value = unknowns * n_sw * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "pixel-updates/s", "value": value, "unit": "pixel-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "square800 GridSolver FP32 Jacobi ('max' gradient, 640,000 unknowns, "
+                               "802x802 crop)", "sweeps_per_step": n_sw, "sweeps_of_full_step": args.sweeps},
+        "cpu_baseline": {"value": value, "unit": "pixel-updates/s", "cores": th, "kind": "port",
+                         "sample": f"{n_sw} of {args.sweeps} sweeps per step, oracle C restatement of the "
+                                   f"reference's Jacobi grid solver (OpenMP, {th} threads)"},
+        "e2e": {"value": value, "unit": "pixel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    from fpie_gb300 import backend, prep
+
+    pb, mc, t, g = square800_inputs()
+    n, m = mc.shape
+    unknowns = int((mc != 0).sum())
+    crop_px = n * m
+    sweeps = args.sweeps
+    stream = torch.cuda.current_stream()
+
+    dm = torch.from_numpy(mc).to(dev)
+    dt_ = torch.from_numpy(t).to(dev)
+    dg = torch.from_numpy(g).to(dev)
+    img = torch.empty((n, m, 3), dtype=torch.uint8, device=dev)
+    err = torch.empty(3, dtype=torch.float32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    s = backend.GridSolver(8, 8)
+    s.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def device_steps(k, solver, reset, finish, record):
+        ev = []
+        for _ in range(k):
+            flush.zero_()  # L2 flush, outside the timed events
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            reset()
+            solver.sweeps(sweeps)
+            e1.record(stream)
+            finish()
+            e2.record(stream)
+            ev.append((e0, e1, e2))
+        if record:
+            torch.cuda.synchronize()
+            return [(a.elapsed_time(c), a.elapsed_time(b)) for a, b, c in ev]
+        return None
+
+    grid_reset = lambda: s.reset_tensors(dm, dt_, dg)  # noqa: E731
+    grid_finish = lambda: s.step_tensors(0, img, err)  # noqa: E731
+
+    device_steps(args.warmup, s, grid_reset, grid_finish, False)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local).start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    l0 = s.launches
+    w0 = time.perf_counter()
+    times = device_steps(args.steps, s, grid_reset, grid_finish, True)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - w0
+    launches = s.launches - l0
+    clk = clocks.stop()
+
+    step_ms = sum(a for a, _ in times)
+    sweep_ms = sum(b for _, b in times)
+    if world > 1:
+        tt = torch.tensor([step_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(tt.item())
+    value = unknowns * sweeps * args.steps * world / (step_ms / 1e3)
+
+    # Parity spot check of the timed path's output against a fresh solve.
+    check = backend.GridSolver(8, 8)
+    check.reset(crop_px, mc, t, g)
+    ref_img, ref_err = check.step(sweeps)
+    same = bool(np.array_equal(img.cpu().numpy(), ref_img))
+
+    # End to end through the plugin API: pinned host inputs, H2D + D2H inside.
+    pin_m = torch.from_numpy(mc).pin_memory()
+    pin_t = torch.from_numpy(t).pin_memory()
+    pin_g = torch.from_numpy(g).pin_memory()
+    hm, ht, hg = pin_m.numpy(), pin_t.numpy(), pin_g.numpy()
+    e2e_solver = backend.GridSolver(8, 8)
+    for _ in range(max(1, min(args.warmup, 3))):
+        e2e_solver.reset(crop_px, hm, ht, hg)
+        e2e_solver.step(sweeps)
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_solver.reset(crop_px, hm, ht, hg)
+        out_img, out_err = e2e_solver.step(sweeps)
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    barrier()
+
+    peak, peak_kind = measured_peak()
+    avg_launch_s = sweep_ms / 1e3 / (args.steps * sweeps)
+    alg_bytes = GRID_BYTES_PER_PX * crop_px
+    achieved = alg_bytes / avg_launch_s / 1e9
+
+    line = {
+        "metric": "pixel-updates/s", "value": value, "unit": "pixel-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms / args.steps,
+        "wall_ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "square800 GridSolver FP32 Jacobi, 5000 sweeps, 'max' gradient "
+                               "(640,000 unknowns, 802x802 crop; 1024^2 target, 900^2 source)",
+                   "unknowns": unknowns, "crop": [n, m], "sweeps": sweeps,
+                   "step": "device reset from HBM-resident inputs + 5000 sweeps + residual + uint8 image",
+                   "l2": "flushed between steps by a 512 MiB write outside the timed events",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "gpu_launches": launches,
+        "e2e": {"value": unknowns * sweeps / e2e_dt, "unit": "pixel-updates/s",
+                "h2d_bytes_per_step": int(mc.nbytes + t.nbytes + g.nbytes),
+                "d2h_bytes_per_step": int(out_img.nbytes + out_err.nbytes),
+                "api": "GridSolver.reset(pinned host arrays) + GridSolver.step(5000)",
+                "ms_per_step": e2e_dt * 1e3},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profiled_traffic("grid_sweep_square800"),
+                     "kernel": "grid_sweep_kernel", "bytes_per_launch": alg_bytes,
+                     "avg_launch_us": avg_launch_s * 1e6, "peak_source": f"hbm_gbs ({peak_kind})"},
+        "clocks": clk,
+        "parity": {"timed_output_equals_fresh_solve": same},
+    }
+
+    if not args.no_equ:
+        from fpie_gb300 import backend as B
+
+        q = B.EquSolver(256)
+        q.set_stream(stream.cuda_stream)
+        sysm = prep.equ_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, pb.gradient,
+                               q.partition)
+        qa = torch.from_numpy(sysm.A).to(dev)
+        qx = torch.from_numpy(sysm.X).to(dev)
+        qb = torch.from_numpy(sysm.B).to(dev)
+        qimg = torch.empty((sysm.N, 3), dtype=torch.uint8, device=dev)
+        q_reset = lambda: q.reset_tensors(sysm.N, qa, qx, qb)  # noqa: E731
+        q_finish = lambda: q.step_tensors(0, qimg, err)  # noqa: E731
+        device_steps(args.warmup, q, q_reset, q_finish, False)
+        qsteps = max(3, args.steps // 4)
+        qt = device_steps(qsteps, q, q_reset, q_finish, True)
+        q_ms = sum(a for a, _ in qt)
+        q_sweep = sum(b for _, b in qt) / 1e3 / (qsteps * sweeps)
+        line["equ"] = {"value": (sysm.N - 1) * sweeps * qsteps / (q_ms / 1e3), "unit": "pixel-updates/s",
+                       "ms_per_step": q_ms / qsteps, "steps": qsteps,
+                       "sweep_kernel_achieved_gbs": EQU_BYTES_PER_UNKNOWN * sysm.N / q_sweep / 1e9}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_grid(mc, t, g)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

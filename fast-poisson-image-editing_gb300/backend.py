@@ -1,0 +1,193 @@
+"""fpie solver plugin classes backed by the GB300 CUDA library.
+
+``EquSolver`` and ``GridSolver`` have the methods, arguments, dtypes and
+return shapes of the reference's native solver classes (pybind11 exports in
+fpie/core/cuda/solver.cc:3-15 over fpie/core/base_solver.h), so
+``EquProcessor`` / ``GridProcessor`` drive them unchanged:
+
+* ``EquSolver(block_size)``: ``partition(mask) -> int32[n,m]``,
+  ``reset(N, A int32[N,4], X f32[N,3], B f32[N,3])``, ``sync()``,
+  ``step(iteration) -> (uint8[N,3], float32[3])``.
+* ``GridSolver(grid_x, grid_y)``: ``reset(N, mask int32[n,m], tgt f32[n,m,3],
+  grad f32[n,m,3])``, ``sync()``, ``step(iteration) -> (uint8[n,m,3],
+  float32[3])``.
+
+Inputs are copied at ``reset`` (the caller may reuse its arrays); ``step``
+continues from the previous state and returns fresh arrays.  Extra methods
+hand device buffers over without host copies (``reset_tensors`` /
+``step_tensors``, torch CUDA tensors) and expose the unclipped FP32 state
+(``state()``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import FPIE_FP32, FPIE_MIXED_BF16, FPIE_MIXED_FP16
+
+PRECISIONS = {"fp32": FPIE_FP32, "fp16": FPIE_MIXED_FP16, "bf16": FPIE_MIXED_BF16}
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _as(a, dtype, shape=None, name="array") -> np.ndarray:
+    out = np.ascontiguousarray(np.asarray(a), dtype=dtype)
+    if shape is not None:
+        if out.ndim != len(shape) or any(s is not None and d != s for d, s in zip(out.shape, shape)):
+            raise _abi.FpieArgumentError(f"{name} has shape {out.shape}, expected {shape}")
+    return out
+
+
+def _tensor_ptr(t, dtype_name: str, name: str) -> int:
+    if not t.is_cuda:
+        raise _abi.FpieArgumentError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise _abi.FpieArgumentError(f"{name} must be contiguous")
+    if str(t.dtype) != f"torch.{dtype_name}":
+        raise _abi.FpieArgumentError(f"{name} must be {dtype_name}, got {t.dtype}")
+    return t.data_ptr()
+
+
+class _Solver:
+    _kind = ""
+
+    def __init__(self) -> None:
+        self._h = ctypes.c_void_p()
+        self._lib = _abi.lib()
+
+    def _create(self, fn: str, *args) -> None:
+        _abi.call(fn, *args, ctypes.byref(self._h))
+
+    def __del__(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.fpie_destroy(h)
+            except Exception:
+                pass
+            h.value = None
+
+    def close(self) -> None:
+        """Free device memory now instead of at garbage collection."""
+        self.__del__()
+
+    def sync(self) -> None:
+        """Wait for the solver's queued device work (a no-op in the reference)."""
+        _abi.call("fpie_sync", self._h)
+
+    def set_stream(self, stream: int | None) -> None:
+        """Enqueue later work on a cudaStream_t (e.g. torch's ``.cuda_stream``)."""
+        _abi.call("fpie_set_stream", self._h, ctypes.c_void_p(stream or 0))
+
+    def set_precision(self, precision: str) -> None:
+        """'fp32' (default), or the mixed forms 'fp16' / 'bf16'."""
+        if precision not in PRECISIONS:
+            raise _abi.FpieArgumentError(f"unknown precision {precision!r}")
+        _abi.call("fpie_set_precision", self._h, PRECISIONS[precision])
+
+    def sweeps(self, iteration: int) -> None:
+        """Enqueue sweeps only (no residual, no image)."""
+        _abi.call("fpie_sweeps", self._h, int(iteration))
+
+    @property
+    def launches(self) -> int:
+        c = ctypes.c_longlong(0)
+        _abi.call("fpie_launch_count", self._h, ctypes.byref(c))
+        return c.value
+
+
+class EquSolver(_Solver):
+    """Jacobi on relabelled unknowns (fpie/core/base_solver.h:12-75)."""
+
+    def __init__(self, block_size: int = 1024) -> None:
+        super().__init__()
+        self._create("fpie_equ_create", int(block_size))
+        self.N = 0
+
+    def partition(self, mask: np.ndarray) -> np.ndarray:
+        m = _as(mask, np.int32, (None, None), "mask")
+        ids = np.empty(m.shape, np.int32)
+        _abi.call("fpie_equ_partition", self._h, _ptr(m), m.shape[0], m.shape[1], _ptr(ids))
+        return ids
+
+    def reset(self, N: int, A: np.ndarray, X: np.ndarray, B: np.ndarray) -> None:
+        N = int(N)
+        A = _as(A, np.int32, (N, 4), "A")
+        X = _as(X, np.float32, (N, 3), "X")
+        B = _as(B, np.float32, (N, 3), "B")
+        _abi.call("fpie_equ_reset", self._h, N, _ptr(A), _ptr(X), _ptr(B))
+        self.N = N
+
+    def step(self, iteration: int) -> tuple[np.ndarray, np.ndarray]:
+        x = np.empty((self.N, 3), np.uint8)
+        err = np.empty(3, np.float32)
+        _abi.call("fpie_equ_step", self._h, int(iteration), _ptr(x), _ptr(err))
+        return x, err
+
+    def state(self) -> np.ndarray:
+        out = np.empty((self.N, 3), np.float32)
+        _abi.call("fpie_get_state", self._h, _ptr(out))
+        return out
+
+    def reset_tensors(self, N: int, A, X, B) -> None:
+        """reset() from torch CUDA tensors (int32[N,4], float32[N,3] x2)."""
+        _abi.call("fpie_equ_reset_device", self._h, int(N), _tensor_ptr(A, "int32", "A"),
+                  _tensor_ptr(X, "float32", "X"), _tensor_ptr(B, "float32", "B"))
+        self.N = int(N)
+
+    def step_tensors(self, iteration: int, x=None, err=None) -> None:
+        """Enqueue step(); results into torch CUDA tensors uint8[N,3] / float32[3]."""
+        _abi.call("fpie_equ_step_device", self._h, int(iteration),
+                  _tensor_ptr(x, "uint8", "x") if x is not None else None,
+                  _tensor_ptr(err, "float32", "err") if err is not None else None)
+
+
+class GridSolver(_Solver):
+    """Jacobi on the cropped image grid (fpie/core/base_solver.h:77-152)."""
+
+    def __init__(self, grid_x: int = 8, grid_y: int = 8) -> None:
+        super().__init__()
+        self._create("fpie_grid_create", int(grid_x), int(grid_y))
+        self.grid_x, self.grid_y = int(grid_x), int(grid_y)
+        self.N = 0
+        self.shape = (0, 0)
+
+    def reset(self, N: int, mask: np.ndarray, tgt: np.ndarray, grad: np.ndarray) -> None:
+        m = _as(mask, np.int32, (None, None), "mask")
+        n_, m_ = m.shape
+        t = _as(tgt, np.float32, (n_, m_, 3), "tgt")
+        g = _as(grad, np.float32, (n_, m_, 3), "grad")
+        _abi.call("fpie_grid_reset", self._h, int(N), n_, m_, _ptr(m), _ptr(t), _ptr(g))
+        self.N = int(N)
+        self.shape = (n_, m_)
+
+    def step(self, iteration: int) -> tuple[np.ndarray, np.ndarray]:
+        img = np.empty((*self.shape, 3), np.uint8)
+        err = np.empty(3, np.float32)
+        _abi.call("fpie_grid_step", self._h, int(iteration), _ptr(img), _ptr(err))
+        return img, err
+
+    def state(self) -> np.ndarray:
+        out = np.empty((*self.shape, 3), np.float32)
+        _abi.call("fpie_get_state", self._h, _ptr(out))
+        return out
+
+    def reset_tensors(self, mask, tgt, grad) -> None:
+        """reset() from torch CUDA tensors int32[n,m], float32[n,m,3] x2."""
+        n_, m_ = mask.shape
+        _abi.call("fpie_grid_reset_device", self._h, int(n_), int(m_),
+                  _tensor_ptr(mask, "int32", "mask"), _tensor_ptr(tgt, "float32", "tgt"),
+                  _tensor_ptr(grad, "float32", "grad"))
+        self.N = int(n_ * m_)
+        self.shape = (int(n_), int(m_))
+
+    def step_tensors(self, iteration: int, img=None, err=None) -> None:
+        """Enqueue step(); results into torch CUDA tensors uint8[n,m,3] / float32[3]."""
+        _abi.call("fpie_grid_step_device", self._h, int(iteration),
+                  _tensor_ptr(img, "uint8", "img") if img is not None else None,
+                  _tensor_ptr(err, "float32", "err") if err is not None else None)

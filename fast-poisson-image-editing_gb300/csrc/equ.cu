@@ -1,0 +1,392 @@
+// EquSolver backend: Jacobi on the relabelled unknowns through the int32
+// neighbour table A (row 0 is the constant-0 unknown absent neighbours use).
+//
+// Replaces fpie/core/cuda/equ.cu (CudaEquSolver) behind the plugin surface
+// of fpie/core/base_solver.h:12-75.  Strict Jacobi with two state buffers,
+// the numpy backend's order of additions (fpie/np_solver.py:31-54), planar
+// channel arrays, a deterministic residual reduction, checked CUDA calls,
+// and neighbour indices validated before any kernel reads through them.
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace fpie {
+
+// X[c][i] planes, `np` floats apart (N rounded up to 32).
+struct EquGeom {
+  int N;
+  long long np;
+};
+
+__global__ void equ_pack_kernel(EquGeom E, const float* __restrict__ X,
+                                const float* __restrict__ B,
+                                float* __restrict__ x0, float* __restrict__ x1,
+                                float* __restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < E.N;
+       i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      x0[c * E.np + i] = X[i * 3 + c];
+      x1[c * E.np + i] = X[i * 3 + c];
+      b[c * E.np + i] = B[i * 3 + c];
+    }
+  }
+}
+
+// Counts A entries outside [0, N) so no sweep ever gathers out of bounds.
+__global__ void equ_check_kernel(EquGeom E, const int4* __restrict__ A,
+                                 unsigned int* __restrict__ bad) {
+  unsigned int nbad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < E.N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int4 a = A[i];
+    nbad += (unsigned)(a.x < 0 || a.x >= E.N) + (unsigned)(a.y < 0 || a.y >= E.N) +
+            (unsigned)(a.z < 0 || a.z >= E.N) + (unsigned)(a.w < 0 || a.w >= E.N);
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+__global__ void equ_unpack_kernel(EquGeom E, const float* __restrict__ x,
+                                  float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < E.N;
+       i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[i * 3 + c] = x[c * E.np + i];
+  }
+}
+
+// One sweep over all rows (row 0 included, as in the numpy backend; with the
+// processor's inputs it stays 0).  The neighbour gathers are mostly
+// contiguous: left/right are i-1/i+1 and up/down one masked row away.
+__global__ void equ_sweep_kernel(EquGeom E, const int4* __restrict__ A,
+                                 const float* __restrict__ b,
+                                 const float* __restrict__ xin,
+                                 float* __restrict__ xout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E.N) return;
+  const int4 a = __ldg(A + i);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float* xc = xin + c * E.np;
+    float s = __fadd_rn(__ldg(b + c * E.np + i), __ldg(xc + a.x));
+    s = __fadd_rn(s, __ldg(xc + a.y));
+    s = __fadd_rn(s, __ldg(xc + a.z));
+    s = __fadd_rn(s, __ldg(xc + a.w));
+    xout[c * E.np + i] = __fmul_rn(s, 0.25f);
+  }
+}
+
+// Residual partials (B + sum X[A] - 4X, numpy order) and the clipped image.
+__global__ void __launch_bounds__(256)
+equ_finish_kernel(EquGeom E, const int4* __restrict__ A,
+                  const float* __restrict__ b, const float* __restrict__ x,
+                  uint8_t* __restrict__ img, double* __restrict__ parts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[3] = {0.0, 0.0, 0.0};
+  if (i < E.N) {
+    const int4 a = __ldg(A + i);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float* xc = x + c * E.np;
+      float s = __fadd_rn(__ldg(b + c * E.np + i), __ldg(xc + a.x));
+      s = __fadd_rn(s, __ldg(xc + a.y));
+      s = __fadd_rn(s, __ldg(xc + a.z));
+      s = __fadd_rn(s, __ldg(xc + a.w));
+      const float xi = xc[i];
+      acc[c] = fabsf(__fsub_rn(s, __fmul_rn(4.0f, xi)));
+      img[(long long)i * 3 + c] = clip_u8(xi);
+    }
+  }
+  block_sum3(acc[0], acc[1], acc[2]);
+  if (threadIdx.x == 0) {
+    parts[3 * (long long)blockIdx.x + 0] = acc[0];
+    parts[3 * (long long)blockIdx.x + 1] = acc[1];
+    parts[3 * (long long)blockIdx.x + 2] = acc[2];
+  }
+}
+
+static int conv_blocks(long long total) {
+  long long b = (total + 255) / 256;
+  return (int)std::max<long long>(1, std::min<long long>(b, 152 * 32));
+}
+
+struct EquSolverImpl : Solver {
+  int block = 256;
+  bool ready = false;
+  EquGeom E{0, 0};
+  int4* A = nullptr;
+  float* x[2] = {nullptr, nullptr};
+  float* b = nullptr;
+  int cur = 0;
+  uint8_t* d_img = nullptr;
+  double* d_part = nullptr;
+  float* d_err = nullptr;
+  unsigned int* d_bad = nullptr;
+  uint8_t* h_img = nullptr;
+  float* h_err = nullptr;
+  unsigned int* h_bad = nullptr;
+  int nparts = 0;
+  static constexpr int kChunk = 64;
+  cudaGraphExec_t chunk[2] = {nullptr, nullptr};
+
+  explicit EquSolverImpl(int block_size) {
+    kind = 1;
+    if (block_size >= 32 && block_size <= 1024 && block_size % 32 == 0) block = block_size;
+    FPIE_CUDA(cudaGetDevice(&device));
+    FPIE_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+    stream = own_stream;
+    FPIE_CUDA(cudaMallocHost(&h_err, 3 * sizeof(float)));
+    FPIE_CUDA(cudaMallocHost(&h_bad, sizeof(unsigned int)));
+    FPIE_CUDA(cudaMalloc(&d_bad, sizeof(unsigned int)));
+  }
+
+  ~EquSolverImpl() override {
+    release();
+    cudaFree(d_bad);
+    if (h_err) cudaFreeHost(h_err);
+    if (h_bad) cudaFreeHost(h_bad);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+
+  void drop_graphs() {
+    for (auto& e : chunk) {
+      if (e) cudaGraphExecDestroy(e);
+      e = nullptr;
+    }
+  }
+
+  void release() {
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graphs();
+    cudaFree(A);
+    cudaFree(x[0]);
+    cudaFree(x[1]);
+    cudaFree(b);
+    cudaFree(d_img);
+    cudaFree(d_part);
+    cudaFree(d_err);
+    if (h_img) cudaFreeHost(h_img);
+    A = nullptr;
+    x[0] = x[1] = b = nullptr;
+    d_img = nullptr;
+    d_part = nullptr;
+    d_err = nullptr;
+    h_img = nullptr;
+    ready = false;
+  }
+
+  void allocate(int N) {
+    FPIE_REQUIRE(N >= 1, FPIE_ERR_ARG, "N must be at least 1");
+    FPIE_REQUIRE(N <= (1 << 29), FPIE_ERR_ARG, "N too large");
+    if (A && E.N == N) {  // same size: keep buffers and captured graphs
+      cur = 0;
+      ready = false;
+      return;
+    }
+    release();
+    E.N = N;
+    E.np = ((long long)N + 31) / 32 * 32;
+    nparts = (N + 255) / 256;
+    const size_t pb = (size_t)E.np * 3 * sizeof(float);
+    FPIE_CUDA(cudaMalloc(&A, (size_t)N * sizeof(int4)));
+    FPIE_CUDA(cudaMalloc(&x[0], pb));
+    FPIE_CUDA(cudaMalloc(&x[1], pb));
+    FPIE_CUDA(cudaMalloc(&b, pb));
+    FPIE_CUDA(cudaMalloc(&d_img, (size_t)N * 3));
+    FPIE_CUDA(cudaMalloc(&d_part, (size_t)nparts * 3 * sizeof(double)));
+    FPIE_CUDA(cudaMalloc(&d_err, 3 * sizeof(float)));
+    FPIE_CUDA(cudaMallocHost(&h_img, (size_t)N * 3));
+    FPIE_CUDA(cudaMemsetAsync(x[0], 0, pb, stream));
+    FPIE_CUDA(cudaMemsetAsync(x[1], 0, pb, stream));
+    FPIE_CUDA(cudaMemsetAsync(b, 0, pb, stream));
+    cur = 0;
+  }
+
+  // Packs X/B and validates A (already in device memory at this->A).
+  void pack_and_check(const float* dX, const float* dB) {
+    equ_pack_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, dX, dB, x[0], x[1], b);
+    post_launch(this);
+    FPIE_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), stream));
+    equ_check_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, A, d_bad);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(h_bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    if (*h_bad) {
+      release();
+      throw Error{FPIE_ERR_ARG, "A holds " + std::to_string(*h_bad) +
+                                    " neighbour indices outside [0, N)"};
+    }
+    ready = true;
+  }
+
+  void reset_host(int N, const int32_t* hA, const float* hX, const float* hB) {
+    FPIE_REQUIRE(hA && hX && hB, FPIE_ERR_ARG, "null input array");
+    allocate(N);
+    float* stage = nullptr;
+    FPIE_CUDA(cudaMallocAsync(&stage, (size_t)N * 24, stream));
+    FPIE_CUDA(cudaMemcpyAsync(A, hA, (size_t)N * 16, cudaMemcpyHostToDevice, stream));
+    FPIE_CUDA(cudaMemcpyAsync(stage, hX, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+    FPIE_CUDA(cudaMemcpyAsync(stage + (size_t)N * 3, hB, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+    pack_and_check(stage, stage + (size_t)N * 3);
+    FPIE_CUDA(cudaFreeAsync(stage, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  void reset_device(int N, const int32_t* dA, const float* dX, const float* dB) {
+    FPIE_REQUIRE(dA && dX && dB, FPIE_ERR_ARG, "null input array");
+    allocate(N);
+    FPIE_CUDA(cudaMemcpyAsync(A, dA, (size_t)N * 16, cudaMemcpyDeviceToDevice, stream));
+    pack_and_check(dX, dB);
+  }
+
+  void sweep_once(cudaStream_t st, int from) {
+    equ_sweep_kernel<<<(E.N + block - 1) / block, block, 0, st>>>(E, A, b, x[from], x[from ^ 1]);
+  }
+
+  void capture_chunk(int start) {
+    cudaStream_t cs = nullptr;
+    cudaGraph_t graph = nullptr;
+    FPIE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      int c = start;
+      for (int k = 0; k < kChunk; ++k, c ^= 1) sweep_once(cs, c);
+      e = cudaStreamEndCapture(cs, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&chunk[start], graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    FPIE_CUDA(e);
+  }
+
+  void run_sweeps(int iters) {
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "step called before reset");
+    while (iters >= kChunk) {
+      if (!chunk[cur]) capture_chunk(cur);
+      FPIE_CUDA(cudaGraphLaunch(chunk[cur], stream));
+      post_launch(this, kChunk);
+      iters -= kChunk;
+    }
+    for (; iters > 0; --iters) {
+      sweep_once(stream, cur);
+      post_launch(this);
+      cur ^= 1;
+    }
+  }
+
+  void finish(uint8_t* img, float* err) {
+    equ_finish_kernel<<<nparts, 256, 0, stream>>>(E, A, b, x[cur], img ? img : d_img, d_part);
+    post_launch(this);
+    launch_finalize(d_part, nparts, err ? err : d_err, stream);
+    post_launch(this);
+  }
+
+  void step_host(int iteration, uint8_t* img_out, float* err_out) {
+    FPIE_REQUIRE(img_out && err_out, FPIE_ERR_ARG, "null output array");
+    if (!ready) {
+      err_out[0] = err_out[1] = err_out[2] = 0.0f;
+      return;
+    }
+    run_sweeps(iteration);
+    finish(d_img, d_err);
+    const size_t bytes = (size_t)E.N * 3;
+    FPIE_CUDA(cudaMemcpyAsync(h_img, d_img, bytes, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaMemcpyAsync(h_err, d_err, 3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy(img_out, h_img, bytes);
+    std::memcpy(err_out, h_err, 3 * sizeof(float));
+  }
+
+  void get_state(float* out) {
+    FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
+    float* tmp = nullptr;
+    FPIE_CUDA(cudaMallocAsync(&tmp, (size_t)E.N * 12, stream));
+    equ_unpack_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, x[cur], tmp);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(out, tmp, (size_t)E.N * 12, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaFreeAsync(tmp, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+  }
+};
+
+Solver* new_equ_solver(int block_size) { return new EquSolverImpl(block_size); }
+
+static EquSolverImpl* equ_of(fpie_solver* s) {
+  return static_cast<EquSolverImpl*>(check_handle(s, 1));
+}
+
+void grid_sweeps(Solver* s, int iters);
+void grid_get_state(Solver* s, float* out);
+
+}  // namespace fpie
+
+using namespace fpie;
+
+extern "C" {
+
+int fpie_equ_partition(fpie_solver* s, const int32_t* mask, int n, int m,
+                       int32_t* ids_out) {
+  return guarded([&] {
+    equ_of(s);
+    FPIE_REQUIRE(mask && ids_out, FPIE_ERR_ARG, "null array");
+    FPIE_REQUIRE(n >= 0 && m >= 0, FPIE_ERR_ARG, "negative mask shape");
+    int32_t cnt = 0;
+    const long long total = (long long)n * m;
+    for (long long k = 0; k < total; ++k) ids_out[k] = mask[k] > 0 ? ++cnt : 0;
+  });
+}
+
+int fpie_equ_reset(fpie_solver* s, int N, const int32_t* A, const float* X,
+                   const float* B) {
+  return guarded([&] { equ_of(s)->reset_host(N, A, X, B); });
+}
+
+int fpie_equ_step(fpie_solver* s, int iteration, uint8_t* x_out, float* err_out) {
+  return guarded([&] { equ_of(s)->step_host(iteration, x_out, err_out); });
+}
+
+int fpie_equ_reset_device(fpie_solver* s, int N, const int32_t* A,
+                          const float* X, const float* B) {
+  return guarded([&] { equ_of(s)->reset_device(N, A, X, B); });
+}
+
+int fpie_equ_step_device(fpie_solver* s, int iteration, uint8_t* x, float* err) {
+  return guarded([&] {
+    EquSolverImpl* h = equ_of(s);
+    h->run_sweeps(iteration);
+    if (x || err) h->finish(x, err);
+  });
+}
+
+int fpie_sweeps(fpie_solver* s, int iteration) {
+  return guarded([&] {
+    Solver* h = check_handle(s, 0);
+    if (h->kind == 1)
+      static_cast<EquSolverImpl*>(h)->run_sweeps(iteration);
+    else
+      grid_sweeps(h, iteration);
+  });
+}
+
+int fpie_get_state(fpie_solver* s, float* out) {
+  return guarded([&] {
+    Solver* h = check_handle(s, 0);
+    if (h->kind == 1)
+      static_cast<EquSolverImpl*>(h)->get_state(out);
+    else
+      grid_get_state(h, out);
+  });
+}
+
+int fpie_set_precision(fpie_solver* s, int precision) {
+  return guarded([&] {
+    Solver* h = check_handle(s, 0);
+    FPIE_REQUIRE(precision == FPIE_FP32, FPIE_ERR_ARG,
+                 "this solver supports FPIE_FP32 only");
+    h->precision = precision;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+"""Host-side construction of solver inputs (the producer of the hot path).
+
+Same semantics as the reference processors' ``reset`` (fpie/process.py),
+bit for bit:
+
+* mask: a 3-channel mask is averaged over channels and compared with 128
+  (for integer masks this is ``channel sum >= 384``), the 1-pixel frame is
+  cleared, and the problem is cropped to the set pixels' bounding box grown
+  by one pixel (fpie/process.py:310-325, :439-452);
+* gradient mixing 'src' / 'avg' / 'max' (BaseProcessor.mixgrad,
+  fpie/process.py:214-223), with ties in 'max' keeping the source term;
+* grid inputs: grad = mixed(C-U) + mixed(C-D) + mixed(C-L) + mixed(C-R)
+  summed in that order, zero outside the mask (fpie/process.py:455-479);
+* equation inputs: ids in row-major order, A = ids of (up, down, left,
+  right), grad summed (L, R, U, D), B = grad + target values of unmasked
+  neighbours added (U, L, R, D), row 0 the constant 0 (fpie/process.py:
+  281-372).
+"""
+
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Crop:
+    x0: int
+    x1: int
+    y0: int
+    y1: int
+
+
+def binary_mask(mask: np.ndarray) -> np.ndarray:
+    """int32 0/1 mask with the outer frame cleared."""
+    if mask.ndim == 3:
+        if np.issubdtype(mask.dtype, np.integer):
+            sel = mask.sum(axis=-1, dtype=np.int64) >= 384
+        else:
+            sel = mask.mean(axis=-1) >= 128
+    else:
+        sel = mask >= 128
+    out = np.zeros(sel.shape, np.int32)
+    out[1:-1, 1:-1] = sel[1:-1, 1:-1]
+    return out
+
+
+def bounding_crop(m01: np.ndarray) -> Crop:
+    rows = np.any(m01, axis=1)
+    cols = np.any(m01, axis=0)
+    if not rows.any():
+        raise ValueError("the mask selects no pixel (after clearing its 1-pixel frame)")
+    r = np.nonzero(rows)[0]
+    c = np.nonzero(cols)[0]
+    return Crop(int(r[0]) - 1, int(r[-1]) + 2, int(c[0]) - 1, int(c[-1]) + 2)
+
+
+def mix(a: np.ndarray, b: np.ndarray, gradient: str) -> np.ndarray:
+    """Mixed gradient term of source difference a and target difference b."""
+    if gradient == "src":
+        return a
+    if gradient == "avg":
+        return (a + b) / 2
+    if gradient == "max":
+        take_b = np.abs(a) < np.abs(b)
+        a = a.copy()
+        a[take_b] = b[take_b]
+        return a
+    raise ValueError(f"unknown gradient mode {gradient!r}")
+
+
+def _check_offsets(shape, img_shape, off, crop: Crop, name: str) -> None:
+    if (off[0] + crop.x0 < 0 or off[1] + crop.y0 < 0
+            or off[0] + crop.x1 > img_shape[0] or off[1] + crop.y1 > img_shape[1]):
+        raise ValueError(
+            f"mask of shape {shape} at offset {tuple(off)} does not fit the {name} "
+            f"image of shape {img_shape[:2]}")
+
+
+def grid_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient):
+    """Return (mask int32[n,m], tgt f32[n,m,3], grad f32[n,m,3], Crop on target)."""
+    m01 = binary_mask(mask)
+    cr = bounding_crop(m01)
+    _check_offsets(mask.shape[:2], src.shape, mask_on_src, cr, "source")
+    _check_offsets(mask.shape[:2], tgt.shape, mask_on_tgt, cr, "target")
+    mc = m01[cr.x0:cr.x1, cr.y0:cr.y1]
+    s = src[mask_on_src[0] + cr.x0:mask_on_src[0] + cr.x1,
+            mask_on_src[1] + cr.y0:mask_on_src[1] + cr.y1].astype(np.float32)
+    t = tgt[mask_on_tgt[0] + cr.x0:mask_on_tgt[0] + cr.x1,
+            mask_on_tgt[1] + cr.y0:mask_on_tgt[1] + cr.y1].astype(np.float32)
+    grad = np.zeros(t.shape, np.float32)
+    # Vertical differences between rows i and i+1, then horizontal ones.
+    dv_s, dv_t = s[1:] - s[:-1], t[1:] - t[:-1]
+    grad[1:] += mix(dv_s, dv_t, gradient)          # centre minus up
+    grad[:-1] += mix(-dv_s, -dv_t, gradient)       # centre minus down
+    dh_s, dh_t = s[:, 1:] - s[:, :-1], t[:, 1:] - t[:, :-1]
+    grad[:, 1:] += mix(dh_s, dh_t, gradient)       # centre minus left
+    grad[:, :-1] += mix(-dh_s, -dh_t, gradient)    # centre minus right
+    grad[mc == 0] = 0
+    on_tgt = Crop(mask_on_tgt[0] + cr.x0, mask_on_tgt[0] + cr.x1,
+                  mask_on_tgt[1] + cr.y0, mask_on_tgt[1] + cr.y1)
+    return mc, t, grad, on_tgt
+
+
+@dataclasses.dataclass
+class EquSystem:
+    N: int
+    A: np.ndarray
+    X: np.ndarray
+    B: np.ndarray
+    tgt_index: tuple[np.ndarray, np.ndarray]
+
+
+def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) -> EquSystem:
+    """Build A/X/B; ``partition`` is the solver's id assignment (mask -> ids)."""
+    m01 = binary_mask(mask)
+    cr = bounding_crop(m01)
+    _check_offsets(mask.shape[:2], src.shape, mask_on_src, cr, "source")
+    _check_offsets(mask.shape[:2], tgt.shape, mask_on_tgt, cr, "target")
+    mc = m01[cr.x0:cr.x1, cr.y0:cr.y1]
+    ids = np.asarray(partition(mc)).astype(np.int64)
+    ids[mc == 0] = 0
+    px, py = np.nonzero(mc)
+    order = np.argsort(ids[px, py], kind="stable")
+    px, py = px[order], py[order]
+    N = px.size + 1
+    sx, sy = px + mask_on_src[0] + cr.x0, py + mask_on_src[1] + cr.y0
+    tx, ty = px + mask_on_tgt[0] + cr.x0, py + mask_on_tgt[1] + cr.y0
+    sc = src[sx, sy].astype(np.float32)
+    tc = tgt[tx, ty].astype(np.float32)
+    grad = None
+    for dx, dy in ((0, -1), (0, 1), (-1, 0), (1, 0)):  # L, R, U, D
+        term = mix(sc - src[sx + dx, sy + dy].astype(np.float32),
+                   tc - tgt[tx + dx, ty + dy].astype(np.float32), gradient)
+        grad = term if grad is None else grad + term
+    A = np.zeros((N, 4), np.int32)
+    X = np.zeros((N, 3), np.float32)
+    B = np.zeros((N, 3), np.float32)
+    X[1:] = tc
+    for k, (dx, dy) in enumerate(((-1, 0), (1, 0), (0, -1), (0, 1))):  # U, D, L, R
+        A[1:, k] = ids[px + dx, py + dy]
+    B[1:] = grad
+    for dx, dy in ((-1, 0), (0, -1), (0, 1), (1, 0)):  # U, L, R, D
+        outside = mc[px + dx, py + dy] == 0
+        B[1:][outside] += tgt[tx + dx, ty + dy][outside].astype(np.float32)
+    return EquSystem(N, A, X, B, (tx, ty))

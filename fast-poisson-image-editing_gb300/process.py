@@ -1,0 +1,142 @@
+"""Processors and backend routing, mirroring ``fpie.process``.
+
+``EquProcessor`` / ``GridProcessor`` take the same constructor arguments as
+the reference's (fpie/process.py:247-279, :384-420), build the solver inputs
+on the host (``prep``), hand them to the backend solver through the plugin
+surface (``partition`` / ``reset`` / ``sync`` / ``step``) and merge the
+solver's uint8 result into a copy of the target (fpie/process.py:374-381,
+:489-496).
+
+Backends (``ALL_BACKEND``, printed by ``--check-backend``):
+
+* ``gb300``      -- plain FP32 Jacobi on the GB300 kernels;
+* ``gb300-fp16`` -- iterative refinement, FP16 correction sweeps;
+* ``gb300-bf16`` -- iterative refinement, BF16 correction sweeps.
+
+An unknown or unavailable backend prints a hint and raises AssertionError,
+as the reference does (fpie/process.py:190-206).
+"""
+
+from __future__ import annotations
+
+import os
+from abc import ABC, abstractmethod
+from typing import Any
+
+import numpy as np
+
+from . import prep
+
+DEFAULT_CPU_CAP = 8
+
+
+def _default_cpu_count() -> int:
+    counts = [c for c in (os.cpu_count(),) if c]
+    try:
+        counts.append(len(os.sched_getaffinity(0)))
+    except (AttributeError, OSError):
+        pass
+    return max(1, min(min(counts), DEFAULT_CPU_CAP)) if counts else 1
+
+
+CPU_COUNT = _default_cpu_count()
+_PRECISION_OF = {"gb300": "fp32", "gb300-fp16": "fp16", "gb300-bf16": "bf16"}
+ALL_BACKEND = list(_PRECISION_OF)
+DEFAULT_BACKEND = "gb300"
+
+_HINTS = {
+    "gb300": "The gb300 backend needs its CUDA library (fpie_gb300.build.build()) "
+             "and a visible GPU.",
+}
+
+
+def _make_core(kind: str, backend: str, block_size: int, grid_x: int, grid_y: int):
+    if backend not in _PRECISION_OF:
+        return None
+    from . import backend as _backend  # the native library loads here
+
+    core = _backend.EquSolver(block_size) if kind == "equ" else _backend.GridSolver(grid_x, grid_y)
+    if _PRECISION_OF[backend] != "fp32":
+        core.set_precision(_PRECISION_OF[backend])
+    return core
+
+
+class BaseProcessor(ABC):
+    """State shared by both processors: gradient mode, rank and the core."""
+
+    def __init__(self, gradient: str, rank: int, backend: str, core: Any | None):
+        if core is None:
+            print(_HINTS.get(backend.split("-")[0], f"Unknown backend {backend!r}; "
+                             f"available: {ALL_BACKEND}"))
+            raise AssertionError(f"Invalid backend {backend}.")
+        self.gradient = gradient
+        self.rank = rank
+        self.backend = backend
+        self.core = core
+        self.root = rank == 0
+
+    def mixgrad(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        return prep.mix(a, b, self.gradient)
+
+    @abstractmethod
+    def reset(self, src: np.ndarray, mask: np.ndarray, tgt: np.ndarray,
+              mask_on_src: tuple[int, int], mask_on_tgt: tuple[int, int]) -> int:
+        ...
+
+    def sync(self) -> None:
+        self.core.sync()
+
+    @abstractmethod
+    def step(self, iteration: int) -> tuple[np.ndarray, np.ndarray] | None:
+        ...
+
+
+class EquProcessor(BaseProcessor):
+    """Equation-form processor: unknowns relabelled, neighbour table A."""
+
+    def __init__(self, gradient: str = "max", backend: str = DEFAULT_BACKEND,
+                 n_cpu: int = CPU_COUNT, min_interval: int = 100, block_size: int = 1024):
+        super().__init__(gradient, 0, backend, _make_core("equ", backend, block_size, 8, 8))
+
+    def mask2index(self, mask: np.ndarray):
+        """ids, N, and the unknowns' (row, col) in id order (fpie/process.py:281-291)."""
+        ids = np.asarray(self.core.partition(mask)).astype(np.int64)
+        ids[mask == 0] = 0
+        x, y = np.nonzero(mask)
+        order = np.argsort(ids[x, y], kind="stable")
+        return ids, x.size + 1, x[order], y[order]
+
+    def reset(self, src, mask, tgt, mask_on_src, mask_on_tgt) -> int:
+        system = prep.equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, self.gradient,
+                                 self.core.partition)
+        self.tgt = tgt.copy()
+        self.tgt_index = system.tgt_index
+        self.core.reset(system.N, system.A, system.X, system.B)
+        return system.N
+
+    def step(self, iteration: int):
+        x, err = self.core.step(iteration)
+        self.tgt[self.tgt_index] = x[1:]
+        return self.tgt, err
+
+
+class GridProcessor(BaseProcessor):
+    """Grid-form processor: the cropped image with its mask."""
+
+    def __init__(self, gradient: str = "max", backend: str = DEFAULT_BACKEND,
+                 n_cpu: int = CPU_COUNT, min_interval: int = 100, block_size: int = 1024,
+                 grid_x: int = 8, grid_y: int = 8):
+        super().__init__(gradient, 0, backend, _make_core("grid", backend, block_size, grid_x, grid_y))
+
+    def reset(self, src, mask, tgt, mask_on_src, mask_on_tgt) -> int:
+        mc, t, grad, crop = prep.grid_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, self.gradient)
+        self.x0, self.x1, self.y0, self.y1 = crop.x0, crop.x1, crop.y0, crop.y1
+        self.tgt = tgt.copy()
+        n = int(mc.shape[0] * mc.shape[1])
+        self.core.reset(n, mc, t, grad)
+        return n
+
+    def step(self, iteration: int):
+        img, err = self.core.step(iteration)
+        self.tgt[self.x0:self.x1, self.y0:self.y1] = img
+        return self.tgt, err

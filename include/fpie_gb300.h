@@ -1,0 +1,139 @@
+/*
+ * fpie_gb300 -- C ABI of the GB300 Jacobi Poisson solver backend for fpie.
+ *
+ * The reference binds its native solvers to Python with pybind11 classes
+ * (fpie/core/cuda/solver.cc:3-15): EquSolver(block_size) with
+ * partition/reset/sync/step and GridSolver(grid_x, grid_y) with
+ * reset/sync/step, on top of the base classes in fpie/core/base_solver.h.
+ * This header is the same surface as plain C: an opaque solver handle, host
+ * pointers and sizes, an int status (0 = success) and a thread-local error
+ * message.  Arrays are C-contiguous in the layouts the reference uses:
+ *   grid mask  int32[n][m],  grid tgt/grad float32[n][m][3],
+ *   equ A      int32[N][4],  equ X/B       float32[N][3],
+ *   images     uint8, same shape as the state they come from.
+ * Every CUDA error is checked and reported through the status; nothing falls
+ * back to the CPU.
+ */
+#ifndef FPIE_GB300_H_
+#define FPIE_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fpie_solver fpie_solver;
+
+enum fpie_status {
+  FPIE_OK = 0,
+  FPIE_ERR_ARG = 1,      /* invalid argument (shape, index, null pointer) */
+  FPIE_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+  FPIE_ERR_STATE = 3,    /* call not valid in the solver's current state */
+  FPIE_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+};
+
+/* Precision of the sweep state (the mixed forms keep an FP32 solution and
+ * solve for an FP16 / BF16 correction by iterative refinement). */
+enum fpie_precision { FPIE_FP32 = 0, FPIE_MIXED_FP16 = 1, FPIE_MIXED_BF16 = 2 };
+
+/* Library version as 10000*major + 100*minor + patch. */
+int fpie_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* fpie_last_error(void);
+
+/* Number of visible CUDA devices (0 is not an error). */
+int fpie_device_count(int* count);
+
+/* ---- EquSolver: fpie/core/base_solver.h:12-75, fpie/core/cuda/equ.cu ---- */
+
+/* Replaces CudaEquSolver(block_size) (fpie/core/cuda/equ.cu:7-17).
+ * block_size is the sweep kernel's block size when it is a multiple of 32
+ * in [32,1024]; otherwise the backend's default is used. */
+int fpie_equ_create(int block_size, fpie_solver** out);
+
+/* Replaces EquSolver.partition (fpie/core/cuda/equ.cu:36-54,
+ * fpie/np_solver.py:14-16): ids[i][j] = row-major running count of
+ * mask > 0 at set pixels, 0 elsewhere. */
+int fpie_equ_partition(fpie_solver* s, const int32_t* mask, int n, int m,
+                       int32_t* ids_out);
+
+/* Replaces EquSolver.reset (fpie/core/base_solver.h:27-59 and
+ * CudaEquSolver::post_reset, fpie/core/cuda/equ.cu:56-74).  Copies the
+ * inputs; every A entry must lie in [0, N). */
+int fpie_equ_reset(fpie_solver* s, int N, const int32_t* A, const float* X,
+                   const float* B);
+
+/* Replaces EquSolver.step (fpie/core/cuda/equ.cu:189-211): runs `iteration`
+ * Jacobi sweeps continuing from the current state, then writes the clipped
+ * uint8 state x_out[N][3] and the per-channel sum of |residual| err_out[3]. */
+int fpie_equ_step(fpie_solver* s, int iteration, uint8_t* x_out,
+                  float* err_out);
+
+/* ---- GridSolver: fpie/core/base_solver.h:77-152, fpie/core/cuda/grid.cu -- */
+
+/* Replaces CudaGridSolver(grid_x, grid_y) (fpie/core/cuda/grid.cu:7-17).
+ * grid_x/grid_y are accepted for interface compatibility; tile shapes are
+ * chosen by the backend. */
+int fpie_grid_create(int grid_x, int grid_y, fpie_solver** out);
+
+/* Replaces GridSolver.reset (fpie/core/base_solver.h:101-140 and
+ * CudaGridSolver::post_reset, fpie/core/cuda/grid.cu:33-52).  N is the
+ * caller's unknown count (bookkeeping only, as in the reference); the grid
+ * is n x m. */
+int fpie_grid_reset(fpie_solver* s, int N, int n, int m, const int32_t* mask,
+                    const float* tgt, const float* grad);
+
+/* Replaces GridSolver.step (fpie/core/cuda/grid.cu:133-153): img_out is
+ * uint8[n][m][3]. */
+int fpie_grid_step(fpie_solver* s, int iteration, uint8_t* img_out,
+                   float* err_out);
+
+/* ---- shared ------------------------------------------------------------ */
+
+/* Replaces EquSolver.sync / GridSolver.sync (fpie/core/base_solver.h:61,142),
+ * a no-op there; here it waits for the solver's stream. */
+int fpie_sync(fpie_solver* s);
+
+/* Frees the solver and its device memory (the pybind object's destructor). */
+int fpie_destroy(fpie_solver* s);
+
+/* Runs later calls of this solver on `stream` (a cudaStream_t; NULL = the
+ * solver's own stream).  Lets a caller order the work with its own streams. */
+int fpie_set_stream(fpie_solver* s, void* stream);
+
+/* Selects the sweep precision (default FPIE_FP32).  Takes effect at the
+ * next step; the FP32 solution is kept across changes. */
+int fpie_set_precision(fpie_solver* s, int precision);
+
+/* ---- device-resident forms (torch tensor handoff; no host copies) --------
+ * Same meaning as the calls above, with all array pointers in device memory
+ * of the solver's device.  The *_device step calls only enqueue work on the
+ * solver's stream; img/err may be NULL to skip those outputs. */
+int fpie_grid_reset_device(fpie_solver* s, int n, int m, const int32_t* mask,
+                           const float* tgt, const float* grad);
+int fpie_grid_step_device(fpie_solver* s, int iteration, uint8_t* img,
+                          float* err);
+int fpie_equ_reset_device(fpie_solver* s, int N, const int32_t* A,
+                          const float* X, const float* B);
+int fpie_equ_step_device(fpie_solver* s, int iteration, uint8_t* x,
+                         float* err);
+
+/* Only the sweeps of a step (no residual, no image); for timing the sweep
+ * kernels on their own. */
+int fpie_sweeps(fpie_solver* s, int iteration);
+
+/* Copies the current FP32 state, in the reference layout ([n][m][3] or
+ * [N][3]), to host memory: the unclipped values the numpy backend keeps. */
+int fpie_get_state(fpie_solver* s, float* out);
+
+/* Kernel launches this solver has issued since creation (sweeps, residual,
+ * image, conversions), counted on the host. */
+int fpie_launch_count(fpie_solver* s, long long* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FPIE_GB300_H_ */

@@ -1,0 +1,35 @@
+"""ORACLE (test infrastructure only): import the reference fpie for checking.
+
+Loads the reference's pure-Python package from its source tree (default
+/root/reference, or $FPIE_REFERENCE) as the module ``fpie``, with the compiled
+reference solver modules that oracle/build_ref.sh puts in oracle/_ref/fpie
+on its search path.  Returns None when the tree is absent, so callers skip.
+"""
+
+from __future__ import annotations
+
+import importlib.util
+import os
+import pathlib
+import sys
+
+_HERE = pathlib.Path(__file__).resolve().parent
+
+
+def import_reference():
+    """Return the reference ``fpie.process`` module, or None if unavailable."""
+    root = pathlib.Path(os.environ.get("FPIE_REFERENCE", "/root/reference"))
+    pkg = root / "fpie"
+    if not (pkg / "process.py").exists():
+        return None
+    if "fpie" not in sys.modules:
+        spec = importlib.util.spec_from_file_location(
+            "fpie", pkg / "__init__.py",
+            submodule_search_locations=[str(pkg), str(_HERE / "_ref" / "fpie")],
+        )
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["fpie"] = mod
+        spec.loader.exec_module(mod)
+    import fpie.process  # noqa: E402
+
+    return fpie.process

@@ -1,0 +1,94 @@
+"""EquSolver on the GPU against the oracle, through the C ABI.
+
+States bit for bit (numpy order B + X[A0] + X[A1] + X[A2] + X[A3]); uint8
+images exactly; err within rtol 1e-5 of the oracle's float64 sum.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import cjacobi
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def backend():
+    from fpie_gb300 import backend as b
+
+    return b
+
+
+def test_partition_matches_reference(backend, golden):
+    name, d = golden
+    s = backend.EquSolver(256)
+    mc = d["grid_mask"]
+    ids = s.partition(mc)
+    assert ids.dtype == np.int32 and ids.shape == mc.shape
+    np.testing.assert_array_equal(np.where(mc > 0, ids, 0), d["equ_ids"])
+    np.testing.assert_array_equal(ids[mc > 0], np.cumsum((mc > 0).reshape(-1)).reshape(mc.shape)[mc > 0])
+
+
+def test_golden_cases(backend, golden):
+    name, d = golden
+    s = backend.EquSolver(1024)
+    N = int(d["equ_N"])
+    s.reset(N, d["equ_A"], d["equ_X"], d["equ_B"])
+    idx = d["equ_tgt_index"]
+    x0, y0 = int(d["grid_box"][0]), int(d["grid_box"][2])
+    done = 0
+    cps = [int(k) for k in d["checkpoints"]]
+    for k in cps:
+        x, err = s.step(k - done)
+        done = k
+        assert x.dtype == np.uint8 and x.shape == (N, 3)
+        np.testing.assert_array_equal(x[1:], d[f"equ_img_{k}"][idx[0] - x0, idx[1] - y0])
+        np.testing.assert_allclose(err, d[f"equ_err_{k}"], rtol=1e-4, atol=1e-3)
+    np.testing.assert_array_equal(s.state(), d[f"equ_state_{cps[-1]}"])
+
+
+def test_square800_5000_sweeps_bit_exact(backend):
+    from fpie_gb300 import prep, workloads
+
+    pb = workloads.square800()
+    s = backend.EquSolver(256)
+    sysm = prep.equ_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, pb.gradient, s.partition)
+    s.reset(sysm.N, sysm.A, sysm.X, sysm.B)
+    x, err = s.step(5000)
+    o = cjacobi.CEqu(sysm.A, sysm.X, sysm.B)
+    o.sweep(5000)
+    np.testing.assert_array_equal(s.state(), o.X)
+    np.testing.assert_array_equal(x, o.image())
+    np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
+
+
+def test_out_of_range_neighbour_is_rejected(backend):
+    from fpie_gb300 import _abi
+
+    d = load_golden("smoke6")
+    A = d["equ_A"].copy()
+    A[2, 1] = int(d["equ_N"])  # one past the end
+    s = backend.EquSolver(256)
+    with pytest.raises(_abi.FpieArgumentError):
+        s.reset(int(d["equ_N"]), A, d["equ_X"], d["equ_B"])
+    A[2, 1] = -1
+    with pytest.raises(_abi.FpieArgumentError):
+        s.reset(int(d["equ_N"]), A, d["equ_X"], d["equ_B"])
+    x, err = s.step(3)  # the rejected reset left no state: empty result
+    assert x.shape == (0, 3)
+
+
+def test_continuation(backend):
+    d = load_golden("blob_frame")
+    args = (int(d["equ_N"]), d["equ_A"], d["equ_X"], d["equ_B"])
+    a, b = backend.EquSolver(128), backend.EquSolver(1024)
+    a.reset(*args)
+    b.reset(*args)
+    for k in (3, 64, 1, 2):
+        a.step(k)
+    b.step(70)
+    np.testing.assert_array_equal(a.state(), b.state())
+    np.testing.assert_array_equal(a.state(), d["equ_state_70"])

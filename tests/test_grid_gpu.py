@@ -1,0 +1,125 @@
+"""GridSolver on the GPU against the oracle, through the C ABI.
+
+Tolerances: FP32 states are compared bit for bit (the kernels keep the numpy
+backend's order of additions); uint8 images exactly; the per-channel error
+(a sum over unknowns, reduced in double on the GPU) within rtol 1e-5 of the
+oracle's float64 sum.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import cjacobi, np_jacobi
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def backend():
+    from fpie_gb300 import backend as b
+
+    return b
+
+
+def test_golden_cases(backend, golden):
+    name, d = golden
+    s = backend.GridSolver(8, 8)
+    s.reset(int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
+    done = 0
+    cps = [int(k) for k in d["checkpoints"]]
+    for k in cps:
+        img, err = s.step(k - done)
+        done = k
+        assert img.dtype == np.uint8 and img.shape == d["grid_mask"].shape + (3,)
+        assert err.dtype == np.float32 and err.shape == (3,)
+        np.testing.assert_array_equal(img, d[f"grid_img_{k}"])
+        np.testing.assert_allclose(err, d[f"grid_err_{k}"], rtol=1e-4, atol=1e-3)
+    np.testing.assert_array_equal(s.state(), d[f"grid_state_{cps[-1]}"])
+    o = np_jacobi.GridJacobi(d["grid_mask"], d["grid_tgt"], d["grid_grad"])
+    o.x = d[f"grid_state_{cps[-1]}"].copy()
+    np.testing.assert_allclose(err, o.err64(), rtol=1e-5, atol=1e-3)
+
+
+def test_border_pixels(backend):
+    d = load_golden("grid_border")
+    s = backend.GridSolver(1, 1)
+    s.reset(d["mask"].size, d["mask"], d["tgt"], d["grad"])
+    done = 0
+    for k in (1, 6, 30):
+        img, err = s.step(k - done)
+        done = k
+        np.testing.assert_array_equal(s.state(), d[f"state_{k}"])
+        np.testing.assert_array_equal(img, d[f"img_{k}"])
+        np.testing.assert_allclose(err, d[f"err_{k}"], rtol=1e-5, atol=1e-3)
+
+
+def _square800_grid():
+    from fpie_gb300 import prep, workloads
+
+    pb = workloads.square800()
+    return prep.grid_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, pb.gradient)
+
+
+def test_square800_5000_sweeps_bit_exact(backend):
+    """640k unknowns, 5000 sweeps: state identical to the C oracle's."""
+    mc, t, g, _ = _square800_grid()
+    s = backend.GridSolver(8, 8)
+    s.reset(mc.size, mc, t, g)
+    img, err = s.step(5000)
+    o = cjacobi.CGrid(mc, t, g)
+    o.sweep(5000)
+    np.testing.assert_array_equal(s.state(), o.x)
+    np.testing.assert_array_equal(img, o.image())
+    np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
+
+
+def test_step_continues_and_reset_restarts(backend):
+    d = load_golden("rand24")
+    args = (int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
+    a = backend.GridSolver(8, 8)
+    a.reset(*args)
+    for k in (1, 2, 0, 64, 3, 130):   # mixes graph chunks and single sweeps
+        a.step(k)
+    b = backend.GridSolver(8, 8)
+    b.reset(*args)
+    b.step(200)
+    np.testing.assert_array_equal(a.state(), b.state())
+    a.reset(*args)  # a second reset starts over from the new inputs
+    a.step(50)
+    np.testing.assert_array_equal(a.state(), d["grid_state_50"])
+    img, err = a.step(-3)  # a negative count runs no sweep, like the reference
+    np.testing.assert_array_equal(a.state(), d["grid_state_50"])
+
+
+def test_before_reset_and_bad_args(backend):
+    s = backend.GridSolver(8, 8)
+    img, err = s.step(10)
+    assert img.shape == (0, 0, 3) and np.all(err == 0)
+    from fpie_gb300 import _abi
+
+    with pytest.raises(_abi.FpieArgumentError):
+        s.reset(4, np.ones((2, 2), np.int32), np.zeros((2, 3, 3), np.float32), np.zeros((2, 2, 3), np.float32))
+    with pytest.raises(_abi.FpieArgumentError):
+        s.reset(0, np.ones((0, 5), np.int32), np.zeros((0, 5, 3), np.float32), np.zeros((0, 5, 3), np.float32))
+
+
+def test_tensor_handoff(backend):
+    torch = pytest.importorskip("torch")
+    d = load_golden("circle256")
+    s = backend.GridSolver(8, 8)
+    s.set_stream(torch.cuda.current_stream().cuda_stream)
+    dev = torch.device("cuda", 0)
+    m = torch.from_numpy(d["grid_mask"]).to(dev)
+    t = torch.from_numpy(d["grid_tgt"]).to(dev)
+    g = torch.from_numpy(d["grid_grad"]).to(dev)
+    s.reset_tensors(m, t, g)
+    img = torch.empty(d["grid_mask"].shape + (3,), dtype=torch.uint8, device=dev)
+    err = torch.empty(3, dtype=torch.float32, device=dev)
+    s.step_tensors(100, img, err)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(img.cpu().numpy(), d["grid_img_100"])
+    np.testing.assert_allclose(err.cpu().numpy(), d["grid_err_100"], rtol=1e-4, atol=1e-3)
+    assert s.launches >= 101
