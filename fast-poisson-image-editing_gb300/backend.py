@@ -80,9 +80,10 @@ class _Solver:
         """Wait for the solver's queued device work (a no-op in the reference)."""
         _abi.call("fpie_sync", self._h)
 
-    def set_stream(self, stream: int | None) -> None:
-        """Enqueue later work on a cudaStream_t (e.g. torch's ``.cuda_stream``)."""
-        _abi.call("fpie_set_stream", self._h, ctypes.c_void_p(stream or 0))
+    def set_stream(self, stream: int) -> None:
+        """Enqueue later work on a cudaStream_t, e.g. torch's ``.cuda_stream``
+        (0 is the legacy default stream, torch's default)."""
+        _abi.call("fpie_set_stream", self._h, ctypes.c_void_p(int(stream)))
 
     def set_precision(self, precision: str) -> None:
         """'fp32' (default), or the mixed forms 'fp16' / 'bf16'."""

@@ -92,7 +92,8 @@ int fpie_sync(fpie_solver* s) {
 int fpie_set_stream(fpie_solver* s, void* stream) {
   return guarded([&] {
     Solver* h = check_handle(s, 0);
-    h->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : h->own_stream;
+    // NULL is a valid choice: the legacy default stream (torch's default).
+    h->stream = reinterpret_cast<cudaStream_t>(stream);
   });
 }
 

@@ -99,8 +99,10 @@ int fpie_sync(fpie_solver* s);
 /* Frees the solver and its device memory (the pybind object's destructor). */
 int fpie_destroy(fpie_solver* s);
 
-/* Runs later calls of this solver on `stream` (a cudaStream_t; NULL = the
- * solver's own stream).  Lets a caller order the work with its own streams. */
+/* Runs later calls of this solver on `stream`, a cudaStream_t used as given:
+ * NULL is the CUDA legacy default stream (torch's default stream).  Until
+ * this is called a solver uses a private non-blocking stream.  Lets a caller
+ * order the solver's work with its own (e.g. torch CUDA events). */
 int fpie_set_stream(fpie_solver* s, void* stream);
 
 /* Selects the sweep precision (default FPIE_FP32).  Takes effect at the
