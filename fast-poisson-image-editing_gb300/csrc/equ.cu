@@ -157,7 +157,7 @@ struct EquSolverImpl : Solver {
   }
 
   void release() {
-    if (stream) cudaStreamSynchronize(stream);
+    cudaStreamSynchronize(stream);  // NULL (legacy default stream) included
     drop_graphs();
     cudaFree(A);
     cudaFree(x[0]);

@@ -100,7 +100,7 @@ struct GridSolverImpl : Solver {
   }
 
   void release() {
-    if (stream) cudaStreamSynchronize(stream);
+    cudaStreamSynchronize(stream);  // NULL (legacy default stream) included
     drop_graphs();
     cudaFree(x[0]);
     cudaFree(x[1]);
