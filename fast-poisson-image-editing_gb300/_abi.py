@@ -55,6 +55,8 @@ _PROTOS: dict[str, tuple] = {
     "fpie_sweeps": ([_P, _I], _I),
     "fpie_get_state": ([_P, _P], _I),
     "fpie_launch_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "fpie_grid_set_kernel": ([_P, ctypes.c_char_p], _I),
+    "fpie_grid_kernel": ([_P, ctypes.c_char_p, _I], _I),
 }
 
 

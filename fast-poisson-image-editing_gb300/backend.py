@@ -173,6 +173,16 @@ class GridSolver(_Solver):
         _abi.call("fpie_grid_step", self._h, int(iteration), _ptr(img), _ptr(err))
         return img, err
 
+    def set_kernel(self, name: str) -> None:
+        """Pin the sweep kernel ("auto", "sweep1", or a variant like "r16w8k8")."""
+        _abi.call("fpie_grid_set_kernel", self._h, name.encode())
+
+    @property
+    def kernel(self) -> str:
+        buf = ctypes.create_string_buffer(64)
+        _abi.call("fpie_grid_kernel", self._h, buf, 64)
+        return buf.value.decode()
+
     def state(self) -> np.ndarray:
         out = np.empty((*self.shape, 3), np.float32)
         _abi.call("fpie_get_state", self._h, _ptr(out))

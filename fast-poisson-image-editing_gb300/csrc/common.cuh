@@ -53,7 +53,8 @@ int guarded(F&& body) {
 
 // ---- grid geometry ----------------------------------------------------------
 // The grid state lives in HBM as three planar float32 channel planes with a
-// zero halo of kPad rows above/below and kPad columns left/right of the crop.
+// zero halo of kPad rows above and kPad columns left of the crop, and
+// kPad + slack rows/columns below and right of it.
 // Rows are `pitch` floats apart, pitch a multiple of 32 (128 bytes), so the
 // first crop column of every row is 16-byte aligned.  The halo lets every
 // tile (including its temporal-blocking apron) be read without bounds checks.
@@ -62,19 +63,25 @@ constexpr int kPad = 32;
 struct GridGeom {
   int n, m;          // crop rows, columns
   int pitch;         // floats per padded row
-  int rows;          // n + 2*kPad
+  int rows;          // n + 2*kPad + kSlackRows
   long long plane;   // floats per channel plane (pitch * rows)
   __host__ __device__ long long at(int i, int j) const {
     return (long long)(i + kPad) * pitch + (j + kPad);
   }
 };
 
+// Rows/columns reserved past the crop's far edges beyond kPad, so that the
+// last tile of any temporally blocked variant (tile up to 224 rows / 120
+// columns plus its apron) reads and writes inside the allocation.
+constexpr int kSlackRows = 256;
+constexpr int kSlackCols = 128;
+
 inline GridGeom make_geom(int n, int m) {
   GridGeom g;
   g.n = n;
   g.m = m;
-  g.pitch = ((m + 2 * kPad) + 31) / 32 * 32;
-  g.rows = n + 2 * kPad;
+  g.pitch = ((m + 2 * kPad + kSlackCols) + 31) / 32 * 32;
+  g.rows = n + 2 * kPad + kSlackRows;
   g.plane = (long long)g.pitch * g.rows;
   return g;
 }

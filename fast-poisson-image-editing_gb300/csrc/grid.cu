@@ -11,9 +11,13 @@
 //  * every CUDA call is checked.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "common.cuh"
 #include "grid_kernels.cuh"
+#include "grid_tb.cuh"
 
 namespace fpie {
 
@@ -109,6 +113,10 @@ struct GridSolverImpl : Solver {
     cudaFree(d_img);
     cudaFree(d_part);
     cudaFree(d_err);
+    cudaFree(flags);
+    flags = nullptr;
+    flags_cap = 0;
+    flags_ok = false;
     if (h_img) cudaFreeHost(h_img);
     x[0] = x[1] = g = nullptr;
     mask = nullptr;
@@ -129,9 +137,11 @@ struct GridSolverImpl : Solver {
       // rewritten by the pack kernel.
       cur = 0;
       ready = false;
+      flags_ok = false;  // the new mask may activate other tiles
       return;
     }
     release();
+    if (!pinned) tuned = false;
     G = make_geom(n, m);
     L = grid_launch(G);
     FPIE_REQUIRE(L.sweep_grid.y <= 65535, FPIE_ERR_ARG, "grid has too many rows");
@@ -188,8 +198,52 @@ struct GridSolverImpl : Solver {
     pack(dm, dt, dg);
   }
 
-  void sweep_once(cudaStream_t st, int from) {
-    launch_grid_sweep(L, G, mask, g, x[from], x[from ^ 1], st);
+  // ---- sweep kernels ---------------------------------------------------------
+  // variant: -1 = one sweep per launch (grid_sweep_kernel), k >= 0 = the k-th
+  // temporally blocked variant.  All give bit-identical states.
+  int variant = kDefaultVariant;
+  bool tuned = false;       // kernel chosen by the autotuner (or pinned)
+  bool pinned = false;      // chosen explicitly with fpie_grid_set_kernel
+  uint8_t* flags = nullptr;  // active-tile flags of `variant`
+  int flags_cap = 0, tiles_x = 0, tiles = 0;
+  bool flags_ok = false;
+
+  static constexpr int kDefaultVariant = 1;  // r16w8k8
+
+  int depth() const { return variant < 0 ? 1 : tb_variants()[variant].depth; }
+
+  void ensure_flags() {
+    if (variant < 0 || flags_ok) return;
+    const TbVariant& v = tb_variants()[variant];
+    tiles_x = (G.m + v.tile_w - 1) / v.tile_w;
+    tiles = tiles_x * ((G.n + v.tile_h - 1) / v.tile_h);
+    if (tiles > flags_cap) {
+      cudaFree(flags);
+      flags = nullptr;
+      FPIE_CUDA(cudaMalloc(&flags, tiles));
+      flags_cap = tiles;
+    }
+    launch_tile_flags(G, mask, v.tile_h, v.tile_w, tiles_x, tiles, flags, stream);
+    post_launch(this);
+    flags_ok = true;
+  }
+
+  void select_variant(int v) {
+    if (v != variant) {
+      drop_graphs();
+      flags_ok = false;
+    }
+    variant = v;
+  }
+
+  // k sweeps (k <= depth()) from buffer `from`; flips nothing (caller does).
+  void launch_block(cudaStream_t st, int from, int k) {
+    if (variant < 0) {
+      launch_grid_sweep(L, G, mask, g, x[from], x[from ^ 1], st);
+    } else {
+      const TbVariant& v = tb_variants()[variant];
+      v.launch(G, mask, g, x[from], x[from ^ 1], flags, tiles_x, tiles, k, st);
+    }
   }
 
   void capture_chunk(int start) {
@@ -199,29 +253,119 @@ struct GridSolverImpl : Solver {
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
       int c = start;
-      for (int k = 0; k < kChunk; ++k, c ^= 1) sweep_once(cs, c);
+      const int d = depth();
+      for (int k = 0; k < kChunk; k += d, c ^= 1) launch_block(cs, c, d);
       e = cudaStreamEndCapture(cs, &graph);
     }
-    if (e == cudaSuccess)
-      e = cudaGraphInstantiate(&chunk[start], graph, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&chunk[start], graph, 0);
     if (graph) cudaGraphDestroy(graph);
     cudaStreamDestroy(cs);
     FPIE_CUDA(e);
   }
 
+  // One graph replay = kChunk sweeps; the launch count is even, so the
+  // current buffer is unchanged afterwards.
+  void run_chunk() {
+    ensure_flags();
+    if (!chunk[cur]) capture_chunk(cur);
+    FPIE_CUDA(cudaGraphLaunch(chunk[cur], stream));
+    post_launch(this, kChunk / depth());
+  }
+
+  // Autotuner: times kChunk sweeps of every candidate (real sweeps, so the
+  // state advances exactly as it would with any one kernel) and keeps the
+  // fastest.  The choice is remembered per grid shape for this process.
+  static std::mutex& tune_mutex() {
+    static std::mutex mu;
+    return mu;
+  }
+  static std::map<std::pair<int, int>, int>& tune_cache() {
+    static std::map<std::pair<int, int>, int> c;
+    return c;
+  }
+  static constexpr int kTuneReps = 2;
+
+  int autotune(int iters) {
+    {
+      std::lock_guard<std::mutex> lk(tune_mutex());
+      auto it = tune_cache().find({G.n, G.m});
+      if (it != tune_cache().end()) {
+        select_variant(it->second);
+        tuned = true;
+        return 0;
+      }
+    }
+    const int ncand = (int)tb_variants().size() + 1;
+    if (iters < ncand * (kTuneReps + 1) * kChunk + kChunk) return 0;
+    cudaEvent_t e0, e1;
+    FPIE_CUDA(cudaEventCreate(&e0));
+    FPIE_CUDA(cudaEventCreate(&e1));
+    int best = kDefaultVariant, used = 0;
+    float best_ms = 1e30f;
+    for (int v = -1; v < ncand - 1; ++v) {
+      select_variant(v);
+      run_chunk();  // warm: flags, graph capture, first replay
+      used += kChunk;
+      for (int r = 0; r < kTuneReps; ++r) {
+        FPIE_CUDA(cudaEventRecord(e0, stream));
+        run_chunk();
+        FPIE_CUDA(cudaEventRecord(e1, stream));
+        FPIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        used += kChunk;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = v;
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    select_variant(best);
+    tuned = true;
+    std::lock_guard<std::mutex> lk(tune_mutex());
+    tune_cache()[{G.n, G.m}] = best;
+    return used;
+  }
+
   void run_sweeps(int iters) {
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "step called before reset");
+    if (iters <= 0) return;
+    if (!tuned && !pinned) iters -= autotune(iters);
     while (iters >= kChunk) {
-      if (!chunk[cur]) capture_chunk(cur);
-      FPIE_CUDA(cudaGraphLaunch(chunk[cur], stream));
-      post_launch(this, kChunk);
+      run_chunk();
       iters -= kChunk;
     }
-    for (; iters > 0; --iters) {
-      sweep_once(stream, cur);
+    ensure_flags();
+    while (iters > 0) {
+      const int k = std::min(iters, depth());
+      launch_block(stream, cur, k);
       post_launch(this);
       cur ^= 1;
+      iters -= k;
     }
+  }
+
+  void set_kernel(const std::string& name) {
+    if (name == "auto") {
+      pinned = false;
+      tuned = false;
+      std::lock_guard<std::mutex> lk(tune_mutex());
+      tune_cache().erase({G.n, G.m});
+      return;
+    }
+    int v = -2;
+    if (name == "sweep1") v = -1;
+    for (size_t k = 0; k < tb_variants().size(); ++k)
+      if (name == tb_variants()[k].name) v = (int)k;
+    FPIE_REQUIRE(v != -2, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
+    select_variant(v);
+    pinned = true;
+  }
+
+  std::string kernel_name() const {
+    return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }
 
   void finish(uint8_t* img, float* err) {
@@ -288,6 +432,21 @@ int fpie_grid_step(fpie_solver* s, int iteration, uint8_t* img_out,
 int fpie_grid_reset_device(fpie_solver* s, int n, int m, const int32_t* mask,
                            const float* tgt, const float* grad) {
   return guarded([&] { grid_of(s)->reset_device(n, m, mask, tgt, grad); });
+}
+
+int fpie_grid_set_kernel(fpie_solver* s, const char* name) {
+  return guarded([&] {
+    FPIE_REQUIRE(name != nullptr, FPIE_ERR_ARG, "null kernel name");
+    grid_of(s)->set_kernel(name);
+  });
+}
+
+int fpie_grid_kernel(fpie_solver* s, char* buf, int len) {
+  return guarded([&] {
+    FPIE_REQUIRE(buf != nullptr && len > 0, FPIE_ERR_ARG, "null or empty buffer");
+    const std::string k = grid_of(s)->kernel_name();
+    std::snprintf(buf, (size_t)len, "%s", k.c_str());
+  });
 }
 
 int fpie_grid_step_device(fpie_solver* s, int iteration, uint8_t* img,

@@ -1,0 +1,31 @@
+// Temporally blocked grid sweep variants (grid_tb.cu).
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace fpie {
+
+struct TbVariant {
+  const char* name;
+  int rows_per_thread, warps, depth;  // R, W, K
+  int tile_h, tile_w;                 // output tile: W*R - 2K rows, 128 - 2K columns
+  // Runs ksweeps (<= depth) sweeps xin -> xout on every active tile.
+  void (*launch)(const GridGeom& G, const uint8_t* mask, const float* g,
+                 const float* xin, float* xout, const uint8_t* active,
+                 int tiles_x, int tiles, int ksweeps, cudaStream_t st);
+};
+
+const std::vector<TbVariant>& tb_variants();
+
+// Marks tiles (tile_h x tile_w, row-major, tiles_x per row) holding a masked pixel.
+void launch_tile_flags(const GridGeom& G, const uint8_t* mask, int th, int tw,
+                       int tiles_x, int tiles, uint8_t* flags, cudaStream_t st);
+
+// Largest tile apron and tile extents any variant needs; the grid allocation
+// reserves this much beyond the crop so no variant reads outside it.
+constexpr int kMaxTileH = 256;
+constexpr int kMaxTileW = 128;
+
+}  // namespace fpie

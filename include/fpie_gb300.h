@@ -130,6 +130,16 @@ int fpie_sweeps(fpie_solver* s, int iteration);
  * [N][3]), to host memory: the unclipped values the numpy backend keeps. */
 int fpie_get_state(fpie_solver* s, float* out);
 
+/* Selects the grid sweep kernel by name: "auto" (default: the autotuner
+ * times the candidates on the first long step and keeps the fastest for this
+ * grid shape), "sweep1" (one sweep per launch) or a temporally blocked
+ * variant "r<R>w<W>k<K>" (R rows per thread, W warps, K sweeps per launch).
+ * Every choice gives bit-identical results. */
+int fpie_grid_set_kernel(fpie_solver* s, const char* name);
+
+/* Writes the current grid sweep kernel's name (NUL-terminated) into buf. */
+int fpie_grid_kernel(fpie_solver* s, char* buf, int len);
+
 /* Kernel launches this solver has issued since creation (sweeps, residual,
  * image, conversions), counted on the host. */
 int fpie_launch_count(fpie_solver* s, long long* count);

@@ -123,3 +123,59 @@ def test_tensor_handoff(backend):
     np.testing.assert_array_equal(img.cpu().numpy(), d["grid_img_100"])
     np.testing.assert_allclose(err.cpu().numpy(), d["grid_err_100"], rtol=1e-4, atol=1e-3)
     assert s.launches >= 101
+
+
+KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16"]
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_every_kernel_is_bit_exact(backend, kernel):
+    """Each sweep kernel, pinned, reproduces the reference's numpy states."""
+    d = load_golden("circle256")
+    s = backend.GridSolver(8, 8)
+    s.set_kernel(kernel)
+    s.reset(int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
+    assert s.kernel == kernel
+    done = 0
+    for k in (1, 100, 5000):  # 1, 99 and 4900 sweeps: partial blocks and chunks
+        img, err = s.step(k - done)
+        done = k
+        np.testing.assert_array_equal(img, d[f"grid_img_{k}"])
+        np.testing.assert_allclose(err, d[f"grid_err_{k}"], rtol=1e-4, atol=1e-3)
+    np.testing.assert_array_equal(s.state(), d["grid_state_5000"])
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_sparse_tiles(backend, kernel):
+    """A mostly empty grid: tiles without masked pixels are skipped."""
+    rng = np.random.default_rng(11)
+    n, m = 301, 517
+    mask = np.zeros((n, m), np.int32)
+    mask[5:40, 7:33] = 1          # top-left corner
+    mask[200:290, 400:505] = 1    # bottom-right region
+    mask[150, 260] = 1            # a single pixel
+    mask[n - 1, 100:120] = 1      # on the last row (neighbours outside read 0)
+    tgt = rng.uniform(0, 255, (n, m, 3)).astype(np.float32)
+    grad = rng.uniform(-30, 30, (n, m, 3)).astype(np.float32)
+    grad[mask == 0] = 0
+    s = backend.GridSolver(8, 8)
+    s.set_kernel(kernel)
+    s.reset(n * m, mask, tgt, grad)
+    o = np_jacobi.GridJacobi(mask, tgt, grad)
+    for k in (3, 77, 130):
+        img, err = s.step(k)
+        o.sweep(k)
+        np.testing.assert_array_equal(s.state(), o.x)
+        np.testing.assert_array_equal(img, o.image())
+        np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
+
+
+def test_autotuner_choice_is_reported(backend):
+    mc, t, g, _ = _square800_grid()
+    s = backend.GridSolver(8, 8)
+    s.reset(mc.size, mc, t, g)
+    s.step(2000)
+    assert s.kernel in KERNELS
+    o = cjacobi.CGrid(mc, t, g)
+    o.sweep(2000)
+    np.testing.assert_array_equal(s.state(), o.x)
