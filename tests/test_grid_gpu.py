@@ -122,7 +122,7 @@ def test_tensor_handoff(backend):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(img.cpu().numpy(), d["grid_img_100"])
     np.testing.assert_allclose(err.cpu().numpy(), d["grid_err_100"], rtol=1e-4, atol=1e-3)
-    assert s.launches >= 101
+    assert s.launches >= 4  # pack, sweeps, residual/image, finalize
 
 
 KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16"]
