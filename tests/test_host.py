@@ -85,7 +85,7 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert set(names) <= set(_abi._PROTOS) | {"fpie_grid_step_noalloc"}
+    assert set(names) <= set(_abi._PROTOS)
     assert _abi.lib().fpie_version() >= 100
 
 
