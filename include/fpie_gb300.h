@@ -140,6 +140,33 @@ int fpie_grid_set_kernel(fpie_solver* s, const char* name);
 /* Writes the current grid sweep kernel's name (NUL-terminated) into buf. */
 int fpie_grid_kernel(fpie_solver* s, char* buf, int len);
 
+/* ---- allocation-free grid step ---------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory where they need a step -- code running while a
+ * stream is captured into a CUDA graph, hosts whose device memory is owned
+ * by their own pool allocator, and loops where cudaMalloc/cudaFree's
+ * possible device synchronization is not acceptable.
+ *
+ * Runs `iteration` Jacobi sweeps of a grid given in the reference layout,
+ * all pointers in device memory of the calling thread's current device:
+ * mask int32[n][m]; x float32[n][m][3], the state, updated in place; grad
+ * float32[n][m][3].  Then, if non-NULL, writes the clipped image
+ * img uint8[n][m][3] and the per-channel sum of |residual| err float32[3].
+ * Work is enqueued on `stream` (NULL = legacy default stream).  Results
+ * are bit-identical to GridSolver's after the same sweeps.
+ *
+ * Limit: n*m <= 262,144 pixels (e.g. 512 x 512); larger grids are rejected
+ * with FPIE_ERR_ARG.  The second state buffer and the residual partials
+ * live in a fixed 3 MiB array in the library's device image, held on every
+ * GPU that loads the library until the process exits.  The first call on
+ * a device resolves that array's address and loads the kernels; make it
+ * before any stream capture.  Calls share the array, so calls whose GPU work
+ * may overlap (other streams or threads) must be serialized by the caller.
+ * Nothing here calls cudaMalloc, cudaFree or an allocating library routine. */
+int fpie_grid_step_noalloc(int n, int m, const int32_t* mask, float* x,
+                           const float* grad, int iteration, uint8_t* img,
+                           float* err, void* stream);
+
 /* Kernel launches this solver has issued since creation (sweeps, residual,
  * image, conversions), counted on the host. */
 int fpie_launch_count(fpie_solver* s, long long* count);
