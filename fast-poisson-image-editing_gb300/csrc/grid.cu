@@ -223,7 +223,8 @@ struct GridSolverImpl : Solver {
       FPIE_CUDA(cudaMalloc(&flags, tiles));
       flags_cap = tiles;
     }
-    launch_tile_flags(G, mask, v.tile_h, v.tile_w, tiles_x, tiles, flags, stream);
+    v.prepare();
+    launch_tile_flags(G, mask, v.tile_h, v.tile_w, v.depth, tiles_x, tiles, flags, stream);
     post_launch(this);
     flags_ok = true;
   }

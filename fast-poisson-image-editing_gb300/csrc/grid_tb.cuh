@@ -15,12 +15,15 @@ struct TbVariant {
   void (*launch)(const GridGeom& G, const uint8_t* mask, const float* g,
                  const float* xin, float* xout, const uint8_t* active,
                  int tiles_x, int tiles, int ksweeps, cudaStream_t st);
+  // One-time host set-up (shared-memory opt-in); call before any capture.
+  void (*prepare)();
 };
 
 const std::vector<TbVariant>& tb_variants();
 
-// Marks tiles (tile_h x tile_w, row-major, tiles_x per row) holding a masked pixel.
-void launch_tile_flags(const GridGeom& G, const uint8_t* mask, int th, int tw,
+// Flags tiles (tile_h x tile_w, row-major, tiles_x per row): 0 = no masked
+// pixel in the tile, 2 = the tile and its k-pixel apron fully masked, 1 = other.
+void launch_tile_flags(const GridGeom& G, const uint8_t* mask, int th, int tw, int k,
                        int tiles_x, int tiles, uint8_t* flags, cudaStream_t st);
 
 // Largest tile apron and tile extents any variant needs; the grid allocation

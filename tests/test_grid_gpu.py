@@ -125,7 +125,8 @@ def test_tensor_handoff(backend):
     assert s.launches >= 4  # pack, sweeps, residual/image, finalize
 
 
-KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16"]
+KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16", "r16w10k8s",
+           "r16w12k8s", "r12w16k16s"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
