@@ -186,17 +186,23 @@ TbVariant make_variant(const char* name) {
 
 }  // namespace
 
+void append_packed_variants(std::vector<TbVariant>& v);  // grid_tbp.cu
+
 const std::vector<TbVariant>& tb_variants() {
-  static const std::vector<TbVariant> v = {
-      make_variant<8, 8, 8, false>("r8w8k8"),
-      make_variant<16, 8, 8, false>("r16w8k8"),
-      make_variant<8, 16, 8, false>("r8w16k8"),
-      make_variant<16, 8, 16, false>("r16w8k16"),
-      make_variant<8, 16, 16, false>("r8w16k16"),
-      make_variant<16, 10, 8, true>("r16w10k8s"),
-      make_variant<16, 12, 8, true>("r16w12k8s"),
-      make_variant<12, 16, 16, true>("r12w16k16s"),
-  };
+  static const std::vector<TbVariant> v = [] {
+    std::vector<TbVariant> t = {
+        make_variant<8, 8, 8, false>("r8w8k8"),
+        make_variant<16, 8, 8, false>("r16w8k8"),
+        make_variant<8, 16, 8, false>("r8w16k8"),
+        make_variant<16, 8, 16, false>("r16w8k16"),
+        make_variant<8, 16, 16, false>("r8w16k16"),
+        make_variant<16, 10, 8, true>("r16w10k8s"),
+        make_variant<16, 12, 8, true>("r16w12k8s"),
+        make_variant<12, 16, 16, true>("r12w16k16s"),
+    };
+    append_packed_variants(t);
+    return t;
+  }();
   return v;
 }
 
