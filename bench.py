@@ -57,6 +57,8 @@ def parse_args():
     p.add_argument("--sweeps", type=int, default=SWEEPS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-equ", action="store_true")
+    p.add_argument("--kernel", default="auto",
+                   help="grid sweep kernel ('auto' = autotuned; a name pins one, e.g. for profiling)")
     return p.parse_args()
 
 
@@ -250,6 +252,8 @@ def run_gb300(args):
 
     s = backend.GridSolver(8, 8)
     s.set_stream(stream.cuda_stream)
+    if args.kernel != "auto":
+        s.set_kernel(args.kernel)
 
     def barrier():
         if world > 1:

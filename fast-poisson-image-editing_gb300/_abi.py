@@ -58,6 +58,23 @@ _PROTOS: dict[str, tuple] = {
     "fpie_grid_set_kernel": ([_P, ctypes.c_char_p], _I),
     "fpie_grid_kernel": ([_P, ctypes.c_char_p, _I], _I),
     "fpie_grid_step_noalloc": ([_I, _I, _P, _P, _P, _I, _P, _P, _P], _I),
+    "fpie_residual_norms": ([_P, _P], _I),
+    "fpie_grid_solve": ([_P, ctypes.c_double, _I, _I, ctypes.POINTER(_I)], _I),
+    "fpie_batch_create": ([ctypes.c_double, ctypes.POINTER(_P)], _I),
+    "fpie_batch_destroy": ([_P], _I),
+    "fpie_batch_job_bytes": ([_I, _I, ctypes.POINTER(ctypes.c_double)], _I),
+    "fpie_batch_add": ([_P, _I, _I, _P, _P, _P, _I, ctypes.POINTER(_I)], _I),
+    "fpie_batch_run": ([_P, _I], _I),
+    "fpie_batch_progress": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "fpie_batch_result": ([_P, _I, _P, _P], _I),
+    "fpie_batch_state": ([_P, _I, _P], _I),
+    "fpie_batch_remove": ([_P, _I], _I),
+    "fpie_batch_norms": ([_P, _P, _I, _P], _I),
+    "fpie_batch_memory": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], _I),
+    "fpie_batch_set_kernel": ([_P, ctypes.c_char_p], _I),
+    "fpie_batch_kernel": ([_P, ctypes.c_char_p, _I], _I),
+    "fpie_batch_set_spin_limit": ([_P, ctypes.c_longlong], _I),
+    "fpie_batch_launch_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
 }
 
 

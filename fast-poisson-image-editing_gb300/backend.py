@@ -183,6 +183,19 @@ class GridSolver(_Solver):
         _abi.call("fpie_grid_kernel", self._h, buf, 64)
         return buf.value.decode()
 
+    def residual_norms(self) -> tuple[np.ndarray, np.ndarray]:
+        """(max |r| per channel, sum |r| per channel) of the current state, FP64."""
+        out = np.empty(6, np.float64)
+        _abi.call("fpie_residual_norms", self._h, _ptr(out))
+        return out[:3].copy(), out[3:].copy()
+
+    def solve(self, tol: float, max_sweeps: int, check_every: int = 256) -> int:
+        """Sweep until every channel's max |residual| <= tol (or max_sweeps); return sweeps run."""
+        done = ctypes.c_int(0)
+        _abi.call("fpie_grid_solve", self._h, float(tol), int(max_sweeps), int(check_every),
+                  ctypes.byref(done))
+        return done.value
+
     def state(self) -> np.ndarray:
         out = np.empty((*self.shape, 3), np.float32)
         _abi.call("fpie_get_state", self._h, _ptr(out))

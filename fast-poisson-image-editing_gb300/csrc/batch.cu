@@ -1,0 +1,655 @@
+// Batched form: many paste jobs of uneven size in one persistent launch.
+//
+// Every job is a grid problem with its own padded planes (the GridSolver
+// layout).  Its sweeps are cut into levels of K sweeps (the tile kernel's
+// temporal depth); a work item is one (job, active tile, channel) at one
+// level.  Items are queued level-major -- all jobs' level 0, then level 1,
+// ... -- and a persistent kernel of (SMs x occupancy) CTAs pulls them with
+// one atomic each.  Before running an item at level z a CTA waits until its
+// job has finished every item of level z-1 (a per-job counter); items of
+// other jobs keep the SMs busy meanwhile, which is what batching buys over
+// one launch per job.  No deadlock is possible: an item is taken only by a
+// running CTA, and every item it waits for was taken earlier by another
+// running CTA that waits only for still earlier levels.  The wait is bounded
+// anyway: past the spin limit the kernel records an error and every CTA
+// leaves, and the host reports FPIE_ERR_TIMEOUT.
+//
+// Arithmetic per pixel is the grid kernels' (numpy order), so each job's
+// result is bit-identical to a GridSolver run of the same sweeps, alone or
+// in any mix.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "grid_kernels.cuh"
+#include "grid_mixed.cuh"
+#include "grid_tbp.cuh"
+
+namespace fpie {
+
+struct BJobDev {
+  GridGeom G;
+  const uint8_t* mask;
+  const float* g;
+  float* x[2];
+  int tiles_x;      // tiles per row of this job
+  int ntiles;       // active tiles
+  int tile_off;     // first entry of this job in the tile list
+  int sweeps;       // sweeps in this launch
+  int parity;       // buffer holding the state at level 0
+};
+
+struct BQueue {
+  const BJobDev* jobs;
+  const int* order;        // jobs sorted by level count, descending
+  const long long* ct;     // ct[k] = items of sorted jobs [0, k)
+  const long long* lo;     // lo[z] = items before level z; lo[nlevels] = total
+  const int* act;          // act[z] = jobs (sorted prefix) still active at level z
+  const int2* tiles;       // (tile index, flag) per job, concatenated
+  int nlevels;
+  unsigned long long* next;
+  int* done;
+  int* error;
+  long long spin_limit;
+};
+
+template <typename T>
+__device__ __forceinline__ int upper_bound_idx(const T* a, int n, T v) {
+  int lo = 0, hi = n;  // first index with a[i] > v
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] <= v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <int R, int W, int K>
+__global__ void __launch_bounds__(W * 32)
+batch_persistent_kernel(BQueue Q) {
+  constexpr int TH = W * R - 2 * K;
+  constexpr int TW = 128 - 2 * K;
+  __shared__ float4 edge[2][2][W][32];
+  __shared__ long long s_idx;
+  __shared__ int s_stop;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long total = Q.lo[Q.nlevels];
+  for (;;) {
+    if (threadIdx.x == 0) s_idx = (long long)atomicAdd(Q.next, 1ULL);
+    __syncthreads();
+    const long long idx = s_idx;
+    if (idx >= total) break;
+    const int z = upper_bound_idx(Q.lo, Q.nlevels + 1, idx) - 1;
+    const long long i = idx - Q.lo[z];
+    const int js = upper_bound_idx(Q.ct, Q.act[z] + 1, i) - 1;
+    const int j = Q.order[js];
+    const BJobDev& J = Q.jobs[j];
+    const int tc = (int)(i - Q.ct[js]);
+    const int ti = tc / 3, c = tc - 3 * ti;
+    if (threadIdx.x == 0) {
+      const int need = J.ntiles * 3 * z;
+      long long spins = 0;
+      int stop = 0;
+      while (*(volatile int*)(Q.done + j) < need) {
+        if (*(volatile int*)Q.error) { stop = 1; break; }
+        if (++spins > Q.spin_limit) {
+          atomicExch(Q.error, 1);
+          stop = 1;
+          break;
+        }
+        __nanosleep(128);
+      }
+      __threadfence();
+      s_stop = stop;
+    }
+    __syncthreads();
+    if (s_stop) break;
+    const int2 tf = Q.tiles[J.tile_off + ti];
+    const int ty = tf.x / J.tiles_x, tx = tf.x - ty * J.tiles_x;
+    const long long base = J.G.at(ty * TH - K + w * R, tx * TW - K + 4 * lane);
+    const int pin = (J.parity + z) & 1;
+    const float* xc = J.x[pin] + c * J.G.plane;
+    float* oc = J.x[pin ^ 1] + c * J.G.plane;
+    const float* gc = J.g + c * J.G.plane;
+    const int ks = min(K, J.sweeps - z * K);
+    if (tf.y == 2)
+      tbp_body<R, W, K, true, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+    else
+      tbp_body<R, W, K, false, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(Q.done + j, 1);
+  }
+}
+
+struct BatchVariant {
+  const char* name;
+  int rows, warps, depth, tile_h, tile_w;
+  const void* kernel;
+  void (*launch)(int grid, const BQueue& q, cudaStream_t st);
+};
+
+template <int R, int W, int K>
+void launch_batch(int grid, const BQueue& q, cudaStream_t st) {
+  batch_persistent_kernel<R, W, K><<<grid, W * 32, 0, st>>>(q);
+}
+
+template <int R, int W, int K>
+BatchVariant make_bv(const char* name) {
+  return BatchVariant{name, R, W, K, W * R - 2 * K, 128 - 2 * K,
+                      (const void*)&batch_persistent_kernel<R, W, K>, &launch_batch<R, W, K>};
+}
+
+static const std::vector<BatchVariant>& batch_variants() {
+  static const std::vector<BatchVariant> v = {
+      make_bv<16, 8, 16>("p16w8k16"),
+      make_bv<8, 16, 16>("p8w16k16"),
+      make_bv<16, 8, 8>("p16w8k8"),
+  };
+  return v;
+}
+
+// ---- host side ---------------------------------------------------------------------
+
+struct BatchJob {
+  int n = 0, m = 0;
+  GridGeom G{};
+  GridLaunch L{};
+  std::vector<uint8_t> hmask;  // 0/1 crop mask, for tile lists
+  float* x[2] = {nullptr, nullptr};
+  float* g = nullptr;
+  uint8_t* mask = nullptr;
+  uint8_t* img = nullptr;
+  double* parts = nullptr;  // per-block partials: 6 doubles each (norms need 6)
+  float* err = nullptr;
+  double* norm = nullptr;   // [max|r| x3, sum|r| x3] of the last norms() call
+  int cur = 0;
+  int sweeps_total = 0, sweeps_done = 0;
+  bool live = false;
+  size_t bytes = 0;
+};
+
+__global__ void batch_pack_kernel(GridGeom G, const int32_t* __restrict__ mk,
+                                  const float* __restrict__ t, const float* __restrict__ gr,
+                                  uint8_t* __restrict__ mask, float* __restrict__ x0,
+                                  float* __restrict__ x1, float* __restrict__ g) {
+  const long long total = (long long)G.n * G.m;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / G.m), j = (int)(idx % G.m);
+    const long long p = G.at(i, j);
+    mask[p] = mk[idx] != 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      x0[c * G.plane + p] = t[idx * 3 + c];
+      x1[c * G.plane + p] = t[idx * 3 + c];
+      g[c * G.plane + p] = gr[idx * 3 + c];
+    }
+  }
+}
+
+struct Batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<BatchJob> jobs;
+  size_t budget = 0, used = 0;
+  int variant = 0;
+  bool tuned = false, pinned = false;
+  long long launches = 0;
+  long long spin_limit = 1LL << 25;  // x ~128 ns sleeps: a few seconds at most
+  int sms = 0;
+
+  explicit Batch(size_t budget_bytes) : budget(budget_bytes) {
+    FPIE_CUDA(cudaGetDevice(&device));
+    FPIE_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    FPIE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  }
+  ~Batch() {
+    cudaStreamSynchronize(stream);
+    for (auto& j : jobs) free_job(j);
+    cudaStreamDestroy(stream);
+  }
+
+  static size_t job_bytes(int n, int m) {
+    const GridGeom G = make_geom(n, m);
+    const GridLaunch L = grid_launch(G);
+    return (size_t)G.plane * (9 * sizeof(float) + 1) + (size_t)n * m * 3 +
+           (size_t)L.nparts * 6 * sizeof(double) + 3 * sizeof(float) + 6 * sizeof(double) +
+           7 * 256;
+  }
+
+  void free_job(BatchJob& j) {
+    cudaFree(j.x[0]);
+    cudaFree(j.x[1]);
+    cudaFree(j.g);
+    cudaFree(j.mask);
+    cudaFree(j.img);
+    cudaFree(j.parts);
+    cudaFree(j.err);
+    cudaFree(j.norm);
+    j.x[0] = j.x[1] = j.g = nullptr;
+    j.mask = j.img = nullptr;
+    j.parts = nullptr;
+    j.err = nullptr;
+    j.norm = nullptr;
+    if (j.live) used -= j.bytes;
+    j.live = false;
+  }
+
+  int add(int n, int m, const int32_t* hm, const float* ht, const float* hg, int iterations) {
+    FPIE_REQUIRE(n >= 1 && m >= 1 && hm && ht && hg, FPIE_ERR_ARG, "bad job arrays");
+    FPIE_REQUIRE(iterations >= 0, FPIE_ERR_ARG, "negative sweep count");
+    FPIE_REQUIRE((long long)n * m <= (1LL << 29), FPIE_ERR_ARG, "job too large");
+    const size_t need = job_bytes(n, m);
+    FPIE_REQUIRE(used + need <= budget, FPIE_ERR_STATE,
+                 "job needs " + std::to_string(need) + " bytes; HBM budget left is " +
+                     std::to_string(budget - used));
+    int id = -1;
+    for (size_t k = 0; k < jobs.size(); ++k)
+      if (!jobs[k].live) { id = (int)k; break; }
+    if (id < 0) { jobs.emplace_back(); id = (int)jobs.size() - 1; }
+    BatchJob& j = jobs[id];
+    j = BatchJob{};
+    j.n = n;
+    j.m = m;
+    j.G = make_geom(n, m);
+    j.L = grid_launch(j.G);
+    j.sweeps_total = iterations;
+    j.sweeps_done = 0;
+    j.hmask.resize((size_t)n * m);
+    for (size_t k = 0; k < j.hmask.size(); ++k) j.hmask[k] = hm[k] != 0;
+    const size_t pb = (size_t)j.G.plane * sizeof(float);
+    try {
+      FPIE_CUDA(cudaMalloc(&j.x[0], 3 * pb));
+      FPIE_CUDA(cudaMalloc(&j.x[1], 3 * pb));
+      FPIE_CUDA(cudaMalloc(&j.g, 3 * pb));
+      FPIE_CUDA(cudaMalloc(&j.mask, (size_t)j.G.plane));
+      FPIE_CUDA(cudaMalloc(&j.img, (size_t)n * m * 3));
+      FPIE_CUDA(cudaMalloc(&j.parts, (size_t)j.L.nparts * 6 * sizeof(double)));
+      FPIE_CUDA(cudaMalloc(&j.err, 3 * sizeof(float)));
+      FPIE_CUDA(cudaMalloc(&j.norm, 6 * sizeof(double)));
+      FPIE_CUDA(cudaMemsetAsync(j.x[0], 0, 3 * pb, stream));
+      FPIE_CUDA(cudaMemsetAsync(j.x[1], 0, 3 * pb, stream));
+      FPIE_CUDA(cudaMemsetAsync(j.g, 0, 3 * pb, stream));
+      FPIE_CUDA(cudaMemsetAsync(j.mask, 0, (size_t)j.G.plane, stream));
+      const size_t px = (size_t)n * m;
+      char* stage = nullptr;
+      FPIE_CUDA(cudaMallocAsync(&stage, px * 28, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage, hm, px * 4, cudaMemcpyHostToDevice, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage + px * 4, ht, px * 12, cudaMemcpyHostToDevice, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage + px * 16, hg, px * 12, cudaMemcpyHostToDevice, stream));
+      const int blocks = (int)std::min<long long>((px + 255) / 256, 152 * 16);
+      batch_pack_kernel<<<blocks, 256, 0, stream>>>(
+          j.G, reinterpret_cast<int32_t*>(stage), reinterpret_cast<float*>(stage + px * 4),
+          reinterpret_cast<float*>(stage + px * 16), j.mask, j.x[0], j.x[1], j.g);
+      FPIE_CUDA(cudaGetLastError());
+      ++launches;
+      FPIE_CUDA(cudaFreeAsync(stage, stream));
+      FPIE_CUDA(cudaStreamSynchronize(stream));  // the caller may reuse its arrays
+    } catch (...) {
+      free_job(j);
+      throw;
+    }
+    j.live = true;
+    j.bytes = need;
+    used += need;
+    return id;
+  }
+
+  BatchJob& job(int id) {
+    FPIE_REQUIRE(id >= 0 && id < (int)jobs.size() && jobs[id].live, FPIE_ERR_ARG,
+                 "no such job " + std::to_string(id));
+    return jobs[id];
+  }
+
+  // (tile index, flag) of the active tiles of a job for a variant's tiling.
+  static void tile_list(const BatchJob& j, const BatchVariant& v, std::vector<int2>& out,
+                        int& tiles_x) {
+    tiles_x = (j.m + v.tile_w - 1) / v.tile_w;
+    const int tiles_y = (j.n + v.tile_h - 1) / v.tile_h;
+    out.clear();
+    for (int ty = 0; ty < tiles_y; ++ty)
+      for (int tx = 0; tx < tiles_x; ++tx) {
+        const int r0 = ty * v.tile_h, c0 = tx * v.tile_w;
+        bool any = false, all = true;
+        for (int i = r0 - v.depth; i < r0 + v.tile_h + v.depth; ++i)
+          for (int k = c0 - v.depth; k < c0 + v.tile_w + v.depth; ++k) {
+            const bool in = i >= 0 && i < j.n && k >= 0 && k < j.m;
+            const bool on = in && j.hmask[(size_t)i * j.m + k];
+            all = all && on;
+            if (on && i >= r0 && i < r0 + v.tile_h && k >= c0 && k < c0 + v.tile_w) any = true;
+          }
+        if (any) out.push_back(make_int2(ty * tiles_x + tx, all ? 2 : 1));
+      }
+  }
+
+  // Runs `sweeps[id]` more sweeps of the listed jobs in one persistent launch
+  // of variant v; returns the device milliseconds (measured with events).
+  float launch(const std::vector<int>& ids, const std::vector<int>& sw, int vi, bool time_it) {
+    const BatchVariant& v = batch_variants()[vi];
+    std::vector<BJobDev> dj;
+    std::vector<int2> tiles, tl;
+    std::vector<int> levels;
+    for (size_t k = 0; k < ids.size(); ++k) {
+      BatchJob& j = jobs[ids[k]];
+      int tx = 0;
+      tile_list(j, v, tl, tx);
+      BJobDev d;
+      d.G = j.G;
+      d.mask = j.mask;
+      d.g = j.g;
+      d.x[0] = j.x[0];
+      d.x[1] = j.x[1];
+      d.tiles_x = tx;
+      d.ntiles = (int)tl.size();
+      d.tile_off = (int)tiles.size();
+      d.sweeps = sw[k];
+      d.parity = j.cur;
+      tiles.insert(tiles.end(), tl.begin(), tl.end());
+      dj.push_back(d);
+      levels.push_back(d.ntiles > 0 ? (sw[k] + v.depth - 1) / v.depth : 0);
+    }
+    const int nj = (int)dj.size();
+    std::vector<int> order(nj);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return levels[a] > levels[b]; });
+    const int nlevels = nj ? levels[order[0]] : 0;
+    std::vector<long long> ct(nj + 1, 0), lo(nlevels + 1, 0);
+    std::vector<int> act(std::max(nlevels, 1), 0);
+    for (int k = 0; k < nj; ++k) ct[k + 1] = ct[k] + 3LL * dj[order[k]].ntiles;
+    for (int z = 0; z < nlevels; ++z) {
+      int a = 0;
+      while (a < nj && levels[order[a]] > z) ++a;
+      act[z] = a;
+      lo[z + 1] = lo[z] + ct[a];
+    }
+    float ms = 0.f;
+    if (nlevels > 0 && lo[nlevels] > 0) {
+      // One device block for the queue tables (freed after the launch).
+      const size_t b_jobs = sizeof(BJobDev) * nj, b_order = sizeof(int) * nj,
+                   b_ct = sizeof(long long) * (nj + 1), b_lo = sizeof(long long) * (nlevels + 1),
+                   b_act = sizeof(int) * nlevels, b_tiles = sizeof(int2) * std::max<size_t>(tiles.size(), 1),
+                   b_done = sizeof(int) * nj;
+      auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+      const size_t bytes = al(b_jobs) + al(b_order) + al(b_ct) + al(b_lo) + al(b_act) +
+                           al(b_tiles) + al(b_done) + 256;
+      std::vector<char> host(bytes, 0);
+      char* dev = nullptr;
+      FPIE_CUDA(cudaMallocAsync(&dev, bytes, stream));
+      size_t off = 0;
+      auto put = [&](const void* src, size_t n) {
+        if (n) std::memcpy(host.data() + off, src, n);
+        const size_t o = off;
+        off += al(n);
+        return dev + o;
+      };
+      BQueue q;
+      q.jobs = reinterpret_cast<const BJobDev*>(put(dj.data(), b_jobs));
+      q.order = reinterpret_cast<const int*>(put(order.data(), b_order));
+      q.ct = reinterpret_cast<const long long*>(put(ct.data(), b_ct));
+      q.lo = reinterpret_cast<const long long*>(put(lo.data(), b_lo));
+      q.act = reinterpret_cast<const int*>(put(act.data(), b_act));
+      q.tiles = reinterpret_cast<const int2*>(put(tiles.data(), sizeof(int2) * tiles.size()));
+      if (tiles.empty()) off += al(sizeof(int2));
+      q.done = reinterpret_cast<int*>(dev + off);
+      off += al(b_done);
+      q.next = reinterpret_cast<unsigned long long*>(dev + off);
+      q.error = reinterpret_cast<int*>(dev + off + 8);
+      q.nlevels = nlevels;
+      q.spin_limit = spin_limit;
+      FPIE_CUDA(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, stream));
+      int occ = 0;
+      FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v.kernel, v.warps * 32, 0));
+      const int grid = std::max(1, occ) * sms;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (time_it) {
+        FPIE_CUDA(cudaEventCreate(&e0));
+        FPIE_CUDA(cudaEventCreate(&e1));
+        FPIE_CUDA(cudaEventRecord(e0, stream));
+      }
+      v.launch(grid, q, stream);
+      FPIE_CUDA(cudaGetLastError());
+      ++launches;
+      if (time_it) FPIE_CUDA(cudaEventRecord(e1, stream));
+      int herr = 0;
+      FPIE_CUDA(cudaMemcpyAsync(&herr, q.error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      FPIE_CUDA(cudaFreeAsync(dev, stream));
+      FPIE_CUDA(cudaStreamSynchronize(stream));
+      if (time_it) {
+        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+      }
+      FPIE_REQUIRE(herr == 0, FPIE_ERR_TIMEOUT,
+                   "batch kernel: a dependency wait exceeded its spin limit");
+    }
+    for (size_t k = 0; k < ids.size(); ++k) {
+      BatchJob& j = jobs[ids[k]];
+      if (levels[k] & 1) j.cur ^= 1;
+      j.sweeps_done += sw[k];
+    }
+    return ms;
+  }
+
+  std::vector<int> live_ids() const {
+    std::vector<int> ids;
+    for (size_t k = 0; k < jobs.size(); ++k)
+      if (jobs[k].live) ids.push_back((int)k);
+    return ids;
+  }
+
+  // Advances every live job by min(limit, its remaining sweeps); limit < 0
+  // means "to completion".  Tunes the kernel on the first call with enough
+  // work (each candidate runs 64 real sweeps of every job).
+  void run(int limit) {
+    std::vector<int> ids = live_ids();
+    auto remaining = [&](int id) {
+      const int rem = jobs[id].sweeps_total - jobs[id].sweeps_done;
+      return limit < 0 ? rem : std::min(rem, limit);
+    };
+    int budget_sweeps = limit;
+    if (!tuned && !pinned) {
+      const int ncand = (int)batch_variants().size();
+      int minrem = 1 << 30;
+      for (int id : ids) minrem = std::min(minrem, remaining(id));
+      if (!ids.empty() && minrem >= 64 * (ncand + 1)) {
+        int best = 0;
+        float best_ms = 1e30f;
+        for (int v = 0; v < ncand; ++v) {
+          std::vector<int> sw(ids.size(), 64);
+          const float ms = launch(ids, sw, v, true);
+          if (ms < best_ms) { best_ms = ms; best = v; }
+        }
+        variant = best;
+        tuned = true;
+        if (budget_sweeps >= 0) budget_sweeps -= 64 * ncand;
+      }
+    }
+    std::vector<int> sw;
+    std::vector<int> run_ids;
+    for (int id : ids) {
+      int rem = jobs[id].sweeps_total - jobs[id].sweeps_done;
+      if (budget_sweeps >= 0) rem = std::min(rem, std::max(0, budget_sweeps));
+      if (rem > 0) { run_ids.push_back(id); sw.push_back(rem); }
+    }
+    if (!run_ids.empty()) launch(run_ids, sw, variant, false);
+  }
+
+  // FP64 residual norms of the listed jobs' current states (one refine
+  // launch + one reduction per job), copied to out[6 * k ...].
+  void norms(const int* ids, int count, double* out) {
+    FPIE_REQUIRE(ids && out && count >= 0, FPIE_ERR_ARG, "bad arguments");
+    std::vector<double> h(6 * (size_t)std::max(count, 1));
+    for (int k = 0; k < count; ++k) {
+      BatchJob& j = job(ids[k]);
+      launch_refine(FPIE_FP32, j.L.sweep_grid, j.L.sweep_block, j.G, j.mask, j.g, j.x[j.cur],
+                    nullptr, nullptr, nullptr, j.parts, stream);
+      launch_norms_finalize(j.parts, j.L.nparts, j.norm, stream);
+      FPIE_CUDA(cudaGetLastError());
+      launches += 2;
+      FPIE_CUDA(cudaMemcpyAsync(h.data() + 6 * (size_t)k, j.norm, 6 * sizeof(double),
+                                cudaMemcpyDeviceToHost, stream));
+    }
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy(out, h.data(), 6 * sizeof(double) * (size_t)count);
+  }
+
+  void finish(int id) {
+    BatchJob& j = job(id);
+    launch_grid_finish(j.L, j.G, j.mask, j.g, j.x[j.cur], j.img, j.parts, stream);
+    launch_finalize(j.parts, j.L.nparts, j.err, stream);
+    FPIE_CUDA(cudaGetLastError());
+    launches += 2;
+  }
+
+  void result(int id, uint8_t* img, float* err) {
+    FPIE_REQUIRE(img && err, FPIE_ERR_ARG, "null output array");
+    BatchJob& j = job(id);
+    finish(id);
+    FPIE_CUDA(cudaMemcpyAsync(img, j.img, (size_t)j.n * j.m * 3, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaMemcpyAsync(err, j.err, 3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  void state(int id, float* out) {
+    FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
+    BatchJob& j = job(id);
+    const size_t plane_bytes = (size_t)j.G.plane * sizeof(float);
+    std::vector<float> h(3 * (size_t)j.G.plane);
+    FPIE_CUDA(cudaMemcpyAsync(h.data(), j.x[j.cur], 3 * plane_bytes, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    for (int i = 0; i < j.n; ++i)
+      for (int k = 0; k < j.m; ++k)
+        for (int c = 0; c < 3; ++c)
+          out[((size_t)i * j.m + k) * 3 + c] = h[(size_t)c * j.G.plane + j.G.at(i, k)];
+  }
+};
+
+}  // namespace fpie
+
+using namespace fpie;
+
+struct fpie_batch;
+
+extern "C" {
+
+int fpie_batch_create(double budget_bytes, fpie_batch** out) {
+  return guarded([&] {
+    FPIE_REQUIRE(out != nullptr, FPIE_ERR_ARG, "null output pointer");
+    FPIE_REQUIRE(budget_bytes > 0, FPIE_ERR_ARG, "budget must be positive");
+    *out = reinterpret_cast<fpie_batch*>(new Batch((size_t)budget_bytes));
+  });
+}
+
+int fpie_batch_destroy(fpie_batch* b) {
+  return guarded([&] {
+    if (b) delete reinterpret_cast<Batch*>(b);
+  });
+}
+
+static Batch* batch_of(fpie_batch* b) {
+  FPIE_REQUIRE(b != nullptr, FPIE_ERR_ARG, "null batch handle");
+  Batch* h = reinterpret_cast<Batch*>(b);
+  FPIE_CUDA(cudaSetDevice(h->device));
+  return h;
+}
+
+int fpie_batch_add(fpie_batch* b, int n, int m, const int32_t* mask, const float* tgt,
+                   const float* grad, int iterations, int* job_id) {
+  return guarded([&] {
+    const int id = batch_of(b)->add(n, m, mask, tgt, grad, iterations);
+    if (job_id) *job_id = id;
+  });
+}
+
+int fpie_batch_job_bytes(int n, int m, double* bytes) {
+  return guarded([&] {
+    FPIE_REQUIRE(bytes && n >= 1 && m >= 1, FPIE_ERR_ARG, "bad arguments");
+    *bytes = (double)Batch::job_bytes(n, m);
+  });
+}
+
+int fpie_batch_run(fpie_batch* b, int max_sweeps) {
+  return guarded([&] { batch_of(b)->run(max_sweeps); });
+}
+
+int fpie_batch_progress(fpie_batch* b, int job, int* done, int* total) {
+  return guarded([&] {
+    BatchJob& j = batch_of(b)->job(job);
+    if (done) *done = j.sweeps_done;
+    if (total) *total = j.sweeps_total;
+  });
+}
+
+int fpie_batch_result(fpie_batch* b, int job, uint8_t* img, float* err) {
+  return guarded([&] { batch_of(b)->result(job, img, err); });
+}
+
+int fpie_batch_state(fpie_batch* b, int job, float* out) {
+  return guarded([&] { batch_of(b)->state(job, out); });
+}
+
+int fpie_batch_norms(fpie_batch* b, const int* jobs, int count, double* out) {
+  return guarded([&] { batch_of(b)->norms(jobs, count, out); });
+}
+
+int fpie_batch_remove(fpie_batch* b, int job) {
+  return guarded([&] {
+    Batch* h = batch_of(b);
+    BatchJob& j = h->job(job);
+    FPIE_CUDA(cudaStreamSynchronize(h->stream));
+    h->free_job(j);
+  });
+}
+
+int fpie_batch_memory(fpie_batch* b, double* used, double* budget) {
+  return guarded([&] {
+    Batch* h = batch_of(b);
+    if (used) *used = (double)h->used;
+    if (budget) *budget = (double)h->budget;
+  });
+}
+
+int fpie_batch_set_kernel(fpie_batch* b, const char* name) {
+  return guarded([&] {
+    Batch* h = batch_of(b);
+    FPIE_REQUIRE(name != nullptr, FPIE_ERR_ARG, "null kernel name");
+    if (std::string(name) == "auto") {
+      h->pinned = false;
+      h->tuned = false;
+      return;
+    }
+    for (size_t k = 0; k < batch_variants().size(); ++k)
+      if (std::string(name) == batch_variants()[k].name) {
+        h->variant = (int)k;
+        h->pinned = true;
+        return;
+      }
+    throw Error{FPIE_ERR_ARG, std::string("unknown batch kernel '") + name + "'"};
+  });
+}
+
+int fpie_batch_kernel(fpie_batch* b, char* buf, int len) {
+  return guarded([&] {
+    FPIE_REQUIRE(buf && len > 0, FPIE_ERR_ARG, "null or empty buffer");
+    std::snprintf(buf, (size_t)len, "%s", batch_variants()[batch_of(b)->variant].name);
+  });
+}
+
+int fpie_batch_set_spin_limit(fpie_batch* b, long long spins) {
+  return guarded([&] {
+    FPIE_REQUIRE(spins > 0, FPIE_ERR_ARG, "spin limit must be positive");
+    batch_of(b)->spin_limit = spins;
+  });
+}
+
+int fpie_batch_launch_count(fpie_batch* b, long long* count) {
+  return guarded([&] {
+    FPIE_REQUIRE(count, FPIE_ERR_ARG, "null pointer");
+    *count = batch_of(b)->launches;
+  });
+}
+
+}  // extern "C"

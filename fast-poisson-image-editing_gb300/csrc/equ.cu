@@ -319,6 +319,7 @@ static EquSolverImpl* equ_of(fpie_solver* s) {
 
 void grid_sweeps(Solver* s, int iters);
 void grid_get_state(Solver* s, float* out);
+void grid_set_precision(Solver* s, int p);
 
 }  // namespace fpie
 
@@ -383,8 +384,12 @@ int fpie_get_state(fpie_solver* s, float* out) {
 int fpie_set_precision(fpie_solver* s, int precision) {
   return guarded([&] {
     Solver* h = check_handle(s, 0);
+    if (h->kind == 2) {
+      grid_set_precision(h, precision);
+      return;
+    }
     FPIE_REQUIRE(precision == FPIE_FP32, FPIE_ERR_ARG,
-                 "this solver supports FPIE_FP32 only");
+                 "EquSolver supports FPIE_FP32 only; the mixed forms are grid solvers");
     h->precision = precision;
   });
 }

@@ -17,6 +17,7 @@
 
 #include "common.cuh"
 #include "grid_kernels.cuh"
+#include "grid_mixed.cuh"
 #include "grid_tb.cuh"
 
 namespace fpie {
@@ -82,6 +83,21 @@ struct GridSolverImpl : Solver {
   static constexpr int kChunk = 64;  // sweeps per captured graph (even)
   cudaGraphExec_t chunk[2] = {nullptr, nullptr};
 
+  // ---- mixed-precision refinement state (allocated on first use) -----------
+  static constexpr int kRefine = 64;  // inner sweeps per refinement cycle
+  void* e[2] = {nullptr, nullptr};    // correction, FP16 or BF16 planes
+  float* r = nullptr;                 // FP32 residual planes
+  double* d_part6 = nullptr;          // per-block max|r|, sum|r| (double)
+  double* d_norm = nullptr;           // [max x3, sum x3]
+  double* h_norm = nullptr;           // pinned copy
+  uint8_t* mflags = nullptr;
+  int mflags_cap = 0, mtiles_x = 0, mtiles = 0;
+  bool mflags_ok = false;
+  int mvariant = 0;
+  bool mtuned = false;
+  int e_prec = -1;                    // precision the e buffers were sized for
+  cudaGraphExec_t cycle[2] = {nullptr, nullptr};
+
   GridSolverImpl(int gx, int gy) : grid_x(gx), grid_y(gy) {
     kind = 2;
     FPIE_CUDA(cudaGetDevice(&device));
@@ -93,14 +109,35 @@ struct GridSolverImpl : Solver {
   ~GridSolverImpl() override {
     release();
     if (h_err) cudaFreeHost(h_err);
+    if (h_norm) cudaFreeHost(h_norm);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
   void drop_graphs() {
-    for (auto& e : chunk) {
-      if (e) cudaGraphExecDestroy(e);
-      e = nullptr;
+    for (auto& gx : chunk) {
+      if (gx) cudaGraphExecDestroy(gx);
+      gx = nullptr;
     }
+    for (auto& gx : cycle) {
+      if (gx) cudaGraphExecDestroy(gx);
+      gx = nullptr;
+    }
+  }
+
+  void release_mixed() {
+    cudaFree(e[0]);
+    cudaFree(e[1]);
+    cudaFree(r);
+    cudaFree(d_part6);
+    cudaFree(d_norm);
+    cudaFree(mflags);
+    e[0] = e[1] = nullptr;
+    r = nullptr;
+    d_part6 = d_norm = nullptr;
+    mflags = nullptr;
+    mflags_cap = 0;
+    mflags_ok = false;
+    e_prec = -1;
   }
 
   void release() {
@@ -117,6 +154,7 @@ struct GridSolverImpl : Solver {
     flags = nullptr;
     flags_cap = 0;
     flags_ok = false;
+    release_mixed();
     if (h_img) cudaFreeHost(h_img);
     x[0] = x[1] = g = nullptr;
     mask = nullptr;
@@ -138,6 +176,7 @@ struct GridSolverImpl : Solver {
       cur = 0;
       ready = false;
       flags_ok = false;  // the new mask may activate other tiles
+      mflags_ok = false;
       return;
     }
     release();
@@ -201,14 +240,20 @@ struct GridSolverImpl : Solver {
   // ---- sweep kernels ---------------------------------------------------------
   // variant: -1 = one sweep per launch (grid_sweep_kernel), k >= 0 = the k-th
   // temporally blocked variant.  All give bit-identical states.
-  int variant = kDefaultVariant;
+  int variant = default_variant();
   bool tuned = false;       // kernel chosen by the autotuner (or pinned)
   bool pinned = false;      // chosen explicitly with fpie_grid_set_kernel
   uint8_t* flags = nullptr;  // active-tile flags of `variant`
   int flags_cap = 0, tiles_x = 0, tiles = 0;
   bool flags_ok = false;
 
-  static constexpr int kDefaultVariant = 1;  // r16w8k8
+  // The kernel used before (or without) autotuning: the packed 16-row,
+  // 8-warp, 16-sweep variant, fastest on both benchmark shapes measured.
+  static int default_variant() {
+    for (size_t k = 0; k < tb_variants().size(); ++k)
+      if (std::string(tb_variants()[k].name) == "p16w8k16") return (int)k;
+    return 0;
+  }
 
   int depth() const { return variant < 0 ? 1 : tb_variants()[variant].depth; }
 
@@ -301,7 +346,7 @@ struct GridSolverImpl : Solver {
     cudaEvent_t e0, e1;
     FPIE_CUDA(cudaEventCreate(&e0));
     FPIE_CUDA(cudaEventCreate(&e1));
-    int best = kDefaultVariant, used = 0;
+    int best = default_variant(), used = 0;
     float best_ms = 1e30f;
     for (int v = -1; v < ncand - 1; ++v) {
       select_variant(v);
@@ -333,6 +378,10 @@ struct GridSolverImpl : Solver {
   void run_sweeps(int iters) {
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "step called before reset");
     if (iters <= 0) return;
+    if (precision != FPIE_FP32) {
+      run_mixed(iters);
+      return;
+    }
     if (!tuned && !pinned) iters -= autotune(iters);
     while (iters >= kChunk) {
       run_chunk();
@@ -348,12 +397,212 @@ struct GridSolverImpl : Solver {
     }
   }
 
+  // ---- mixed precision ---------------------------------------------------------
+  void ensure_mixed() {
+    if (e[0] == nullptr || e_prec != precision) {
+      release_mixed();
+      const size_t eb = (size_t)G.plane * 3 * 2;  // FP16 / BF16
+      FPIE_CUDA(cudaMalloc(&e[0], eb));
+      FPIE_CUDA(cudaMalloc(&e[1], eb));
+      FPIE_CUDA(cudaMalloc(&r, (size_t)G.plane * 3 * sizeof(float)));
+      FPIE_CUDA(cudaMalloc(&d_part6, (size_t)L.nparts * 6 * sizeof(double)));
+      FPIE_CUDA(cudaMalloc(&d_norm, 6 * sizeof(double)));
+      FPIE_CUDA(cudaMemsetAsync(e[0], 0, eb, stream));
+      FPIE_CUDA(cudaMemsetAsync(e[1], 0, eb, stream));
+      FPIE_CUDA(cudaMemsetAsync(r, 0, (size_t)G.plane * 3 * sizeof(float), stream));
+      e_prec = precision;
+      drop_graphs();
+    }
+    if (!mflags_ok) {
+      const MixedVariant& v = mixed_variants()[mvariant];
+      mtiles_x = (G.m + v.tile_w - 1) / v.tile_w;
+      mtiles = mtiles_x * ((G.n + v.tile_h - 1) / v.tile_h);
+      if (mtiles > mflags_cap) {
+        cudaFree(mflags);
+        mflags = nullptr;
+        FPIE_CUDA(cudaMalloc(&mflags, mtiles));
+        mflags_cap = mtiles;
+      }
+      launch_tile_flags(G, mask, v.tile_h, v.tile_w, v.depth, mtiles_x, mtiles, mflags, stream);
+      post_launch(this);
+      mflags_ok = true;
+    }
+  }
+
+  void select_mixed(int v) {
+    if (v != mvariant) {
+      drop_graphs();
+      mflags_ok = false;
+    }
+    mvariant = v;
+  }
+
+  // FP64 norms of the residual of x[cur] (no fold) into d_norm.
+  void refine_norms(cudaStream_t st, float* rout) {
+    launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[cur], nullptr,
+                  nullptr, rout, d_part6, st);
+    launch_norms_finalize(d_part6, L.nparts, d_norm, st);
+  }
+
+  // One cycle from x parity `xc`: c inner sweeps on e (from 0), then fold
+  // e into x[xc ^ 1] and compute the new residual and norms.
+  void mixed_cycle(cudaStream_t st, int xc, int c) {
+    const MixedVariant& v = mixed_variants()[mvariant];
+    const MixedVariant::Launch fn =
+        precision == FPIE_MIXED_BF16 ? v.launch_bf16 : v.launch_fp16;
+    int last = 0;
+    for (int done = 0, k = 0; done < c; done += k) {
+      k = std::min(c - done, v.depth);
+      const int out = done == 0 ? 0 : last ^ 1;
+      fn(G, mask, r, done == 0 ? nullptr : e[last], e[out], mflags, mtiles_x, mtiles, k,
+         done == 0 ? 1 : 0, st);
+      last = out;
+    }
+    launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[xc], e[last],
+                  x[xc ^ 1], r, d_part6, st);
+    launch_norms_finalize(d_part6, L.nparts, d_norm, st);
+  }
+
+  int cycle_launches(int c) const {
+    const int d = mixed_variants()[mvariant].depth;
+    return (c + d - 1) / d + 2;
+  }
+
+  void run_cycle_graph() {
+    if (!cycle[cur]) {
+      cudaStream_t cs = nullptr;
+      cudaGraph_t graph = nullptr;
+      FPIE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      cudaError_t err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      if (err == cudaSuccess) {
+        mixed_cycle(cs, cur, kRefine);
+        err = cudaStreamEndCapture(cs, &graph);
+      }
+      if (err == cudaSuccess) err = cudaGraphInstantiate(&cycle[cur], graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      cudaStreamDestroy(cs);
+      FPIE_CUDA(err);
+    }
+    FPIE_CUDA(cudaGraphLaunch(cycle[cur], stream));
+    post_launch(this, cycle_launches(kRefine));
+    cur ^= 1;
+  }
+
+  int autotune_mixed(int iters) {
+    const std::pair<int, int> key{G.n * 4 + precision, G.m};
+    {
+      std::lock_guard<std::mutex> lk(tune_mutex());
+      auto it = mixed_tune_cache().find(key);
+      if (it != mixed_tune_cache().end()) {
+        select_mixed(it->second);
+        mtuned = true;
+        return 0;
+      }
+    }
+    const int ncand = (int)mixed_variants().size();
+    if (iters < ncand * (kTuneReps + 1) * kRefine + kRefine) return 0;
+    cudaEvent_t e0, e1;
+    FPIE_CUDA(cudaEventCreate(&e0));
+    FPIE_CUDA(cudaEventCreate(&e1));
+    int best = 0, used = 0;
+    float best_ms = 1e30f;
+    for (int v = 0; v < ncand; ++v) {
+      select_mixed(v);
+      ensure_mixed();
+      run_cycle_graph();
+      used += kRefine;
+      for (int rep = 0; rep < kTuneReps; ++rep) {
+        FPIE_CUDA(cudaEventRecord(e0, stream));
+        run_cycle_graph();
+        FPIE_CUDA(cudaEventRecord(e1, stream));
+        FPIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        used += kRefine;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = v;
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    select_mixed(best);
+    mtuned = true;
+    std::lock_guard<std::mutex> lk(tune_mutex());
+    mixed_tune_cache()[key] = best;
+    return used;
+  }
+
+  static std::map<std::pair<int, int>, int>& mixed_tune_cache() {
+    static std::map<std::pair<int, int>, int> c;
+    return c;
+  }
+
+  void run_mixed(int iters) {
+    ensure_mixed();
+    refine_norms(stream, r);  // r of the current x starts the first cycle
+    post_launch(this, 2);
+    if (!mtuned && !pinned) iters -= autotune_mixed(iters);
+    ensure_mixed();
+    while (iters >= kRefine) {
+      run_cycle_graph();
+      iters -= kRefine;
+    }
+    if (iters > 0) {
+      mixed_cycle(stream, cur, iters);
+      post_launch(this, cycle_launches(iters));
+      cur ^= 1;
+    }
+  }
+
+  void residual_norms(double* out) {
+    FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
+    if (!d_part6) {
+      FPIE_CUDA(cudaMalloc(&d_part6, (size_t)L.nparts * 6 * sizeof(double)));
+      FPIE_CUDA(cudaMalloc(&d_norm, 6 * sizeof(double)));
+    }
+    if (!h_norm) FPIE_CUDA(cudaMallocHost(&h_norm, 6 * sizeof(double)));
+    refine_norms(stream, nullptr);
+    post_launch(this, 2);
+    FPIE_CUDA(cudaMemcpyAsync(h_norm, d_norm, 6 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy(out, h_norm, 6 * sizeof(double));
+  }
+
+  // Sweeps in blocks of `check_every` until every channel's max |r| <= tol
+  // or max_sweeps are done; returns the sweeps run.
+  int solve(double tol, int max_sweeps, int check_every) {
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "solve called before reset");
+    FPIE_REQUIRE(check_every > 0 && max_sweeps >= 0, FPIE_ERR_ARG, "bad solve limits");
+    int done = 0;
+    double nrm[6];
+    residual_norms(nrm);
+    while (done < max_sweeps && std::max(nrm[0], std::max(nrm[1], nrm[2])) > tol) {
+      const int k = std::min(check_every, max_sweeps - done);
+      run_sweeps(k);
+      done += k;
+      residual_norms(nrm);
+    }
+    return done;
+  }
+
   void set_kernel(const std::string& name) {
     if (name == "auto") {
       pinned = false;
       tuned = false;
       std::lock_guard<std::mutex> lk(tune_mutex());
       tune_cache().erase({G.n, G.m});
+      return;
+    }
+    if (precision != FPIE_FP32) {
+      int v = -1;
+      for (size_t k = 0; k < mixed_variants().size(); ++k)
+        if (name == mixed_variants()[k].name) v = (int)k;
+      FPIE_REQUIRE(v >= 0, FPIE_ERR_ARG, "unknown mixed-precision grid kernel '" + name + "'");
+      select_mixed(v);
+      pinned = true;
       return;
     }
     int v = -2;
@@ -366,7 +615,18 @@ struct GridSolverImpl : Solver {
   }
 
   std::string kernel_name() const {
+    if (precision != FPIE_FP32) return std::string(mixed_variants()[mvariant].name);
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
+  }
+
+  void set_precision(int p) {
+    FPIE_REQUIRE(p == FPIE_FP32 || p == FPIE_MIXED_FP16 || p == FPIE_MIXED_BF16, FPIE_ERR_ARG,
+                 "unknown precision");
+    if (p != precision) {
+      precision = p;
+      pinned = false;
+      drop_graphs();
+    }
   }
 
   void finish(uint8_t* img, float* err) {
@@ -435,6 +695,18 @@ int fpie_grid_reset_device(fpie_solver* s, int n, int m, const int32_t* mask,
   return guarded([&] { grid_of(s)->reset_device(n, m, mask, tgt, grad); });
 }
 
+int fpie_residual_norms(fpie_solver* s, double* out) {
+  return guarded([&] { grid_of(s)->residual_norms(out); });
+}
+
+int fpie_grid_solve(fpie_solver* s, double tol, int max_sweeps, int check_every,
+                    int* sweeps_done) {
+  return guarded([&] {
+    const int d = grid_of(s)->solve(tol, max_sweeps, check_every);
+    if (sweeps_done) *sweeps_done = d;
+  });
+}
+
 int fpie_grid_set_kernel(fpie_solver* s, const char* name) {
   return guarded([&] {
     FPIE_REQUIRE(name != nullptr, FPIE_ERR_ARG, "null kernel name");
@@ -465,4 +737,5 @@ namespace fpie {
 // Kind-dispatching helpers used by the shared ABI calls in equ.cu.
 void grid_sweeps(Solver* s, int iters) { static_cast<GridSolverImpl*>(s)->run_sweeps(iters); }
 void grid_get_state(Solver* s, float* out) { static_cast<GridSolverImpl*>(s)->get_state(out); }
+void grid_set_precision(Solver* s, int p) { static_cast<GridSolverImpl*>(s)->set_precision(p); }
 }  // namespace fpie

@@ -21,6 +21,19 @@ struct TbVariant {
 
 const std::vector<TbVariant>& tb_variants();
 
+// Packed temporally blocked sweeps on a low-precision correction e
+// (e' = (r + sum of neighbours' e) / 4 on masked pixels, FP32 arithmetic).
+struct MixedVariant {
+  const char* name;
+  int depth, tile_h, tile_w;
+  using Launch = void (*)(const GridGeom& G, const uint8_t* mask, const float* r,
+                          const void* ein, void* eout, const uint8_t* active, int tiles_x,
+                          int tiles, int ksweeps, int zero_start, cudaStream_t st);
+  Launch launch_fp16, launch_bf16;
+};
+
+const std::vector<MixedVariant>& mixed_variants();
+
 // Flags tiles (tile_h x tile_w, row-major, tiles_x per row): 0 = no masked
 // pixel in the tile, 2 = the tile and its k-pixel apron fully masked, 1 = other.
 void launch_tile_flags(const GridGeom& G, const uint8_t* mask, int th, int tw, int k,

@@ -19,111 +19,17 @@
 // 2) take a path without it.  The choice is made once per CTA.
 #include "common.cuh"
 #include "grid_tb.cuh"
+#include "grid_tbp.cuh"
 
 namespace fpie {
 
-__device__ __forceinline__ float2 pick2(uint32_t ma, uint32_t mb, uint32_t bit,
-                                        float2 upd, float2 old) {
-  return make_float2((ma & bit) ? upd.x : old.x, (mb & bit) ? upd.y : old.y);
-}
-
-template <int R, int W, int K, bool FULL>
-__device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __restrict__ mask,
-                                         const float* __restrict__ gc,
-                                         const float* __restrict__ xc, float* __restrict__ oc,
-                                         long long base, int ksweeps, int lane, int w,
-                                         float4 (&edge)[2][2][W][32]) {
-  constexpr int H = R / 2;
-  float2 P[H][4], Gp[H][4];
-  uint32_t mk[R];
-#pragma unroll
-  for (int i = 0; i < H; ++i) {
-    const long long pa = base + (long long)i * G.pitch;
-    const long long pb = base + (long long)(i + H) * G.pitch;
-    const float4 a = ld4(xc + pa), b = ld4(xc + pb);
-    const float4 ga = ld4(gc + pa), gb = ld4(gc + pb);
-    P[i][0] = make_float2(a.x, b.x);
-    P[i][1] = make_float2(a.y, b.y);
-    P[i][2] = make_float2(a.z, b.z);
-    P[i][3] = make_float2(a.w, b.w);
-    Gp[i][0] = make_float2(ga.x, gb.x);
-    Gp[i][1] = make_float2(ga.y, gb.y);
-    Gp[i][2] = make_float2(ga.z, gb.z);
-    Gp[i][3] = make_float2(ga.w, gb.w);
-    if (!FULL) {
-      mk[i] = __ldg(reinterpret_cast<const unsigned int*>(mask + pa));
-      mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
-    }
-  }
-  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float2 q = make_float2(0.25f, 0.25f);
-  for (int s = 0; s < ksweeps; ++s) {
-    const int par = s & 1;
-    edge[par][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
-    edge[par][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
-    __syncthreads();
-    const float4 above = w > 0 ? edge[par][1][w - 1][lane] : zero;
-    const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
-    // Pair 0's up: (row -1 from the warp above, row H-1 own).
-    float2 up[4] = {make_float2(above.x, P[H - 1][0].x), make_float2(above.y, P[H - 1][1].x),
-                    make_float2(above.z, P[H - 1][2].x), make_float2(above.w, P[H - 1][3].x)};
-    // Pair H-1's down: (row H own, row R from the warp below).
-    const float2 dlast[4] = {make_float2(P[0][0].y, below.x), make_float2(P[0][1].y, below.y),
-                             make_float2(P[0][2].y, below.z), make_float2(P[0][3].y, below.w)};
-#pragma unroll
-    for (int i = 0; i < H; ++i) {
-      float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
-      float2 dn[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) dn[j] = i < H - 1 ? P[i + 1][j] : dlast[j];
-      const float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cur[3].x, 1),
-                                    __shfl_up_sync(0xffffffffu, cur[3].y, 1));
-      const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
-                                    __shfl_down_sync(0xffffffffu, cur[0].y, 1));
-      float2 o[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float2 l = j > 0 ? cur[j - 1] : lf;
-        const float2 r = j < 3 ? cur[j + 1] : rt;
-        float2 t = __fadd2_rn(Gp[i][j], up[j]);
-        t = __fadd2_rn(t, dn[j]);
-        t = __fadd2_rn(t, l);
-        t = __fadd2_rn(t, r);
-        o[j] = __fmul2_rn(t, q);
-      }
-      if (!FULL) {
-        o[0] = pick2(mk[i], mk[i + H], 0x000000ffu, o[0], cur[0]);
-        o[1] = pick2(mk[i], mk[i + H], 0x0000ff00u, o[1], cur[1]);
-        o[2] = pick2(mk[i], mk[i + H], 0x00ff0000u, o[2], cur[2]);
-        o[3] = pick2(mk[i], mk[i + H], 0xff000000u, o[3], cur[3]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        up[j] = cur[j];
-        P[i][j] = o[j];
-      }
-    }
-  }
-  if (lane >= K / 4 && lane < 32 - K / 4) {
-#pragma unroll
-    for (int i = 0; i < H; ++i) {
-      const int ra = w * R + i, rb = w * R + i + H;  // region rows
-      if (ra >= K && ra < W * R - K)
-        *reinterpret_cast<float4*>(oc + base + (long long)i * G.pitch) =
-            make_float4(P[i][0].x, P[i][1].x, P[i][2].x, P[i][3].x);
-      if (rb >= K && rb < W * R - K)
-        *reinterpret_cast<float4*>(oc + base + (long long)(i + H) * G.pitch) =
-            make_float4(P[i][0].y, P[i][1].y, P[i][2].y, P[i][3].y);
-    }
-  }
-}
-
-template <int R, int W, int K>
+template <int R, int W, int K, typename TS, bool ZS, bool GS = false>
 __global__ void __launch_bounds__(W * 32)
 grid_tbp_kernel(GridGeom G, const uint8_t* __restrict__ mask,
-                const float* __restrict__ g, const float* __restrict__ xin,
-                float* __restrict__ xout, const uint8_t* __restrict__ active,
+                const float* __restrict__ g, const TS* __restrict__ xin,
+                TS* __restrict__ xout, const uint8_t* __restrict__ active,
                 int tiles_x, int ksweeps) {
+  extern __shared__ float4 tbp_dyn[];
   constexpr int TH = W * R - 2 * K;
   constexpr int TW = 128 - 2 * K;
   static_assert(R % 2 == 0 && R >= 4, "rows per thread must be even");
@@ -137,28 +43,42 @@ grid_tbp_kernel(GridGeom G, const uint8_t* __restrict__ mask,
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
   const long long base = G.at(ty * TH - K + w * R, tx * TW - K + 4 * lane);
-  const float* xc = xin + c * G.plane;
+  const TS* xc = xin + c * G.plane;
   const float* gc = g + c * G.plane;
-  float* oc = xout + c * G.plane;
+  TS* oc = xout + c * G.plane;
+  float2* sg = reinterpret_cast<float2*>(tbp_dyn) + (size_t)w * (R / 2) * 32 * 4;
   if (flag == 2)
-    tbp_body<R, W, K, true>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge);
+    tbp_body<R, W, K, true, TS, ZS, false, GS>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
   else
-    tbp_body<R, W, K, false>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge);
+    tbp_body<R, W, K, false, TS, ZS, false, GS>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
 }
 
 namespace {
 
 void no_prepare() {}
 
-template <int R, int W, int K>
+template <int R, int W, bool GS>
+constexpr size_t tbp_smem() {
+  return GS ? (size_t)W * R * 32 * 4 * sizeof(float2) / 2 : 0;
+}
+
+template <int R, int W, int K, bool GS>
+void prepare_tbp() {
+  if (tbp_smem<R, W, GS>() > 48 * 1024)
+    FPIE_CUDA(cudaFuncSetAttribute(grid_tbp_kernel<R, W, K, float, false, GS>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tbp_smem<R, W, GS>()));
+}
+
+template <int R, int W, int K, bool GS = false>
 void launch_tbp(const GridGeom& G, const uint8_t* mask, const float* g,
                 const float* xin, float* xout, const uint8_t* active,
                 int tiles_x, int tiles, int ksweeps, cudaStream_t st) {
-  grid_tbp_kernel<R, W, K><<<dim3(tiles, 3), W * 32, 0, st>>>(G, mask, g, xin, xout, active,
-                                                             tiles_x, ksweeps);
+  grid_tbp_kernel<R, W, K, float, false, GS><<<dim3(tiles, 3), W * 32, tbp_smem<R, W, GS>(), st>>>(
+      G, mask, g, xin, xout, active, tiles_x, ksweeps);
 }
 
-template <int R, int W, int K>
+template <int R, int W, int K, bool GS = false>
 TbVariant make_packed(const char* name) {
   TbVariant v;
   v.name = name;
@@ -167,19 +87,55 @@ TbVariant make_packed(const char* name) {
   v.depth = K;
   v.tile_h = W * R - 2 * K;
   v.tile_w = 128 - 2 * K;
-  v.launch = &launch_tbp<R, W, K>;
-  v.prepare = &no_prepare;
+  v.launch = &launch_tbp<R, W, K, GS>;
+  v.prepare = GS ? &prepare_tbp<R, W, K, GS> : &no_prepare;
+  return v;
+}
+
+template <int R, int W, int K, typename TS>
+void launch_tbp_lp(const GridGeom& G, const uint8_t* mask, const float* r, const void* ein,
+                   void* eout, const uint8_t* active, int tiles_x, int tiles, int ksweeps,
+                   int zero_start, cudaStream_t st) {
+  if (zero_start)
+    grid_tbp_kernel<R, W, K, TS, true><<<dim3(tiles, 3), W * 32, 0, st>>>(
+        G, mask, r, nullptr, static_cast<TS*>(eout), active, tiles_x, ksweeps);
+  else
+    grid_tbp_kernel<R, W, K, TS, false><<<dim3(tiles, 3), W * 32, 0, st>>>(
+        G, mask, r, static_cast<const TS*>(ein), static_cast<TS*>(eout), active, tiles_x,
+        ksweeps);
+}
+
+template <int R, int W, int K>
+MixedVariant make_mixed(const char* name) {
+  MixedVariant v;
+  v.name = name;
+  v.depth = K;
+  v.tile_h = W * R - 2 * K;
+  v.tile_w = 128 - 2 * K;
+  v.launch_fp16 = &launch_tbp_lp<R, W, K, __half>;
+  v.launch_bf16 = &launch_tbp_lp<R, W, K, __nv_bfloat16>;
   return v;
 }
 
 }  // namespace
 
+const std::vector<MixedVariant>& mixed_variants() {
+  static const std::vector<MixedVariant> v = {
+      make_mixed<16, 8, 16>("p16w8k16"),
+      make_mixed<8, 16, 16>("p8w16k16"),
+      make_mixed<16, 8, 8>("p16w8k8"),
+  };
+  return v;
+}
+
 void append_packed_variants(std::vector<TbVariant>& v) {
   v.push_back(make_packed<16, 8, 8>("p16w8k8"));
   v.push_back(make_packed<16, 8, 16>("p16w8k16"));
   v.push_back(make_packed<8, 16, 16>("p8w16k16"));
-  v.push_back(make_packed<12, 10, 16>("p12w10k16"));
   v.push_back(make_packed<8, 12, 8>("p8w12k8"));
+  v.push_back(make_packed<16, 8, 4>("p16w8k4"));
+  v.push_back(make_packed<12, 12, 8, true>("p12w12k8s"));
+  v.push_back(make_packed<8, 16, 8, true>("p8w16k8s"));
 }
 
 }  // namespace fpie

@@ -1,0 +1,194 @@
+// Packed temporally blocked tile body shared by the launch-per-block
+// kernels (grid_tbp.cu) and the persistent batch kernel (batch.cu).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+
+namespace fpie {
+
+// Loads/stores of 4 consecutive state values in the storage type TS, as
+// float4 (the arithmetic is always FP32).  FP16/BF16 values are 8 bytes per
+// group of 4, so the same 4-aligned indexing keeps every access aligned.
+// CG = true reads through L2 only (ld.global.cg): required when other CTAs
+// of the same launch wrote the data (the persistent batch kernel).
+template <typename TS, bool CG = false>
+struct Lanes4;
+
+template <bool CG>
+struct Lanes4<float, CG> {
+  static __device__ __forceinline__ float4 load(const float* p) {
+    return CG ? __ldcg(reinterpret_cast<const float4*>(p)) : ld4(p);
+  }
+  static __device__ __forceinline__ void store(float* p, float4 v) {
+    *reinterpret_cast<float4*>(p) = v;
+  }
+};
+
+template <bool CG>
+struct Lanes4<__half, CG> {
+  static __device__ __forceinline__ float4 load(const __half* p) {
+    const uint2 u = CG ? __ldcg(reinterpret_cast<const uint2*>(p))
+                       : __ldg(reinterpret_cast<const uint2*>(p));
+    __half2 a, b;
+    memcpy(&a, &u.x, 4);
+    memcpy(&b, &u.y, 4);
+    const float2 fa = __half22float2(a), fb = __half22float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+  }
+  static __device__ __forceinline__ void store(__half* p, float4 v) {
+    const __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+    uint2 u;
+    memcpy(&u.x, &a, 4);
+    memcpy(&u.y, &b, 4);
+    *reinterpret_cast<uint2*>(p) = u;
+  }
+};
+
+template <bool CG>
+struct Lanes4<__nv_bfloat16, CG> {
+  static __device__ __forceinline__ float4 load(const __nv_bfloat16* p) {
+    const uint2 u = CG ? __ldcg(reinterpret_cast<const uint2*>(p))
+                       : __ldg(reinterpret_cast<const uint2*>(p));
+    __nv_bfloat162 a, b;
+    memcpy(&a, &u.x, 4);
+    memcpy(&b, &u.y, 4);
+    const float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+  }
+  static __device__ __forceinline__ void store(__nv_bfloat16* p, float4 v) {
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+    uint2 u;
+    memcpy(&u.x, &a, 4);
+    memcpy(&u.y, &b, 4);
+    *reinterpret_cast<uint2*>(p) = u;
+  }
+};
+
+__device__ __forceinline__ float2 pick2(uint32_t ma, uint32_t mb, uint32_t bit,
+                                        float2 upd, float2 old) {
+  return make_float2((ma & bit) ? upd.x : old.x, (mb & bit) ? upd.y : old.y);
+}
+
+// TS: storage type of the swept state (float for the plain solver; __half
+// or __nv_bfloat16 for the correction of the mixed form).  zero_start: the
+// state starts at 0 instead of being loaded (first inner launch of a
+// refinement cycle).
+// GS: the grad pairs live in shared memory (sg: this warp's H x 32 x 4
+// float2, i.e. W*R*32*16 bytes per CTA, dynamic) instead of registers,
+// freeing 4R registers per thread for taller regions.
+template <int R, int W, int K, bool FULL, typename TS, bool ZS, bool CG = false, bool GS = false>
+__device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __restrict__ mask,
+                                         const float* __restrict__ gc,
+                                         const TS* __restrict__ xc, TS* __restrict__ oc,
+                                         long long base, int ksweeps,
+                                         int lane, int w, float4 (&edge)[2][2][W][32],
+                                         float2* __restrict__ sg = nullptr) {
+  constexpr int H = R / 2;
+  float2 P[H][4], Gp[GS ? 1 : H][4];
+  uint32_t mk[R];
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const long long pa = base + (long long)i * G.pitch;
+    const long long pb = base + (long long)(i + H) * G.pitch;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 a = ZS ? z4 : Lanes4<TS, CG>::load(xc + pa);
+    const float4 b = ZS ? z4 : Lanes4<TS, CG>::load(xc + pb);
+    const float4 ga = ld4(gc + pa), gb = ld4(gc + pb);
+    P[i][0] = make_float2(a.x, b.x);
+    P[i][1] = make_float2(a.y, b.y);
+    P[i][2] = make_float2(a.z, b.z);
+    P[i][3] = make_float2(a.w, b.w);
+    if (GS) {
+      float2* q = sg + ((size_t)i * 32 + lane) * 4;
+      *reinterpret_cast<float4*>(q) = make_float4(ga.x, gb.x, ga.y, gb.y);
+      *reinterpret_cast<float4*>(q + 2) = make_float4(ga.z, gb.z, ga.w, gb.w);
+    } else {
+      Gp[GS ? 0 : i][0] = make_float2(ga.x, gb.x);
+      Gp[GS ? 0 : i][1] = make_float2(ga.y, gb.y);
+      Gp[GS ? 0 : i][2] = make_float2(ga.z, gb.z);
+      Gp[GS ? 0 : i][3] = make_float2(ga.w, gb.w);
+    }
+    if (!FULL) {
+      mk[i] = __ldg(reinterpret_cast<const unsigned int*>(mask + pa));
+      mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
+    }
+  }
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float2 q = make_float2(0.25f, 0.25f);
+  for (int s = 0; s < ksweeps; ++s) {
+    const int par = s & 1;
+    edge[par][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+    edge[par][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+    __syncthreads();
+    const float4 above = w > 0 ? edge[par][1][w - 1][lane] : zero;
+    const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
+    // Pair 0's up: (row -1 from the warp above, row H-1 own).
+    float2 up[4] = {make_float2(above.x, P[H - 1][0].x), make_float2(above.y, P[H - 1][1].x),
+                    make_float2(above.z, P[H - 1][2].x), make_float2(above.w, P[H - 1][3].x)};
+    // Pair H-1's down: (row H own, row R from the warp below).
+    const float2 dlast[4] = {make_float2(P[0][0].y, below.x), make_float2(P[0][1].y, below.y),
+                             make_float2(P[0][2].y, below.z), make_float2(P[0][3].y, below.w)};
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
+      float2 dn[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dn[j] = i < H - 1 ? P[i + 1][j] : dlast[j];
+      const float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cur[3].x, 1),
+                                    __shfl_up_sync(0xffffffffu, cur[3].y, 1));
+      const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
+                                    __shfl_down_sync(0xffffffffu, cur[0].y, 1));
+      float2 gv[4];
+      if (GS) {
+        const float4* q = reinterpret_cast<const float4*>(sg + ((size_t)i * 32 + lane) * 4);
+        const float4 a = q[0], b = q[1];
+        gv[0] = make_float2(a.x, a.y);
+        gv[1] = make_float2(a.z, a.w);
+        gv[2] = make_float2(b.x, b.y);
+        gv[3] = make_float2(b.z, b.w);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) gv[j] = Gp[GS ? 0 : i][j];
+      }
+      float2 o[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float2 l = j > 0 ? cur[j - 1] : lf;
+        const float2 r = j < 3 ? cur[j + 1] : rt;
+        float2 t = __fadd2_rn(gv[j], up[j]);
+        t = __fadd2_rn(t, dn[j]);
+        t = __fadd2_rn(t, l);
+        t = __fadd2_rn(t, r);
+        o[j] = __fmul2_rn(t, q);
+      }
+      if (!FULL) {
+        o[0] = pick2(mk[i], mk[i + H], 0x000000ffu, o[0], cur[0]);
+        o[1] = pick2(mk[i], mk[i + H], 0x0000ff00u, o[1], cur[1]);
+        o[2] = pick2(mk[i], mk[i + H], 0x00ff0000u, o[2], cur[2]);
+        o[3] = pick2(mk[i], mk[i + H], 0xff000000u, o[3], cur[3]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        up[j] = cur[j];
+        P[i][j] = o[j];
+      }
+    }
+  }
+  if (lane >= K / 4 && lane < 32 - K / 4) {
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      const int ra = w * R + i, rb = w * R + i + H;  // region rows
+      if (ra >= K && ra < W * R - K)
+        Lanes4<TS>::store(oc + base + (long long)i * G.pitch,
+                          make_float4(P[i][0].x, P[i][1].x, P[i][2].x, P[i][3].x));
+      if (rb >= K && rb < W * R - K)
+        Lanes4<TS>::store(oc + base + (long long)(i + H) * G.pitch,
+                          make_float4(P[i][0].y, P[i][1].y, P[i][2].y, P[i][3].y));
+    }
+  }
+}
+
+}  // namespace fpie

@@ -53,6 +53,9 @@ _HINTS = {
 def _make_core(kind: str, backend: str, block_size: int, grid_x: int, grid_y: int):
     if backend not in _PRECISION_OF:
         return None
+    if kind == "equ" and _PRECISION_OF[backend] != "fp32":
+        print(f"{backend} is a grid-only backend: use the grid method (GridProcessor).")
+        return None
     from . import backend as _backend  # the native library loads here
 
     core = _backend.EquSolver(block_size) if kind == "equ" else _backend.GridSolver(grid_x, grid_y)

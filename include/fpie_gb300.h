@@ -106,7 +106,11 @@ int fpie_destroy(fpie_solver* s);
 int fpie_set_stream(fpie_solver* s, void* stream);
 
 /* Selects the sweep precision (default FPIE_FP32).  Takes effect at the
- * next step; the FP32 solution is kept across changes. */
+ * next step; the FP32 solution is kept across changes.  The mixed forms
+ * (grid solvers only) run each step as cycles of 64 inner Jacobi sweeps on
+ * a correction stored in FP16 / BF16 (FP32 arithmetic), each cycle
+ * followed by x += e and a fresh FP32 residual; results equal FP32 Jacobi
+ * up to the correction's rounding, not bit for bit. */
 int fpie_set_precision(fpie_solver* s, int precision);
 
 /* ---- device-resident forms (torch tensor handoff; no host copies) --------
@@ -129,6 +133,19 @@ int fpie_sweeps(fpie_solver* s, int iteration);
 /* Copies the current FP32 state, in the reference layout ([n][m][3] or
  * [N][3]), to host memory: the unclipped values the numpy backend keeps. */
 int fpie_get_state(fpie_solver* s, float* out);
+
+/* Per-channel norms of the current state's residual r = grad + sum of
+ * neighbours - 4x over masked pixels (grid solvers): out[0..2] = max |r|,
+ * out[3..5] = sum |r|, reduced in FP64 on the GPU.  Synchronizes. */
+int fpie_residual_norms(fpie_solver* s, double* out);
+
+/* Grid solvers: sweeps in blocks of check_every until every channel's
+ * max |r| <= tol, or max_sweeps are done; *sweeps_done (may be NULL)
+ * receives the count.  Works in every precision; for the mixed forms
+ * check_every is best a multiple of 64 (one refinement cycle).  No
+ * counterpart in the reference, whose step() always runs a fixed count. */
+int fpie_grid_solve(fpie_solver* s, double tol, int max_sweeps, int check_every,
+                    int* sweeps_done);
 
 /* Selects the grid sweep kernel by name: "auto" (default: the autotuner
  * times the candidates on the first long step and keeps the fastest for this
@@ -166,6 +183,46 @@ int fpie_grid_kernel(fpie_solver* s, char* buf, int len);
 int fpie_grid_step_noalloc(int n, int m, const int32_t* mask, float* x,
                            const float* grad, int iteration, uint8_t* img,
                            float* err, void* stream);
+
+/* ---- batched form: many uneven grid jobs in one persistent launch --------
+ * No counterpart in the reference (which solves one paste per process).
+ * A batch owns device memory for its jobs up to `budget_bytes`; each job is
+ * a grid problem in the GridSolver layouts plus its own sweep count.
+ * fpie_batch_run advances every job by min(max_sweeps, its remaining
+ * sweeps) (max_sweeps < 0: to completion) in one persistent kernel whose
+ * CTAs pull (job, tile, channel, level) items from a queue; the first run
+ * with enough work autotunes the tile shape and temporal depth on real
+ * sweeps.  A job's result is bit-identical to a GridSolver run of the same
+ * sweeps.  Dependency waits inside the kernel are bounded: past the spin
+ * limit the call returns FPIE_ERR_TIMEOUT and the jobs' states are
+ * undefined (remove and re-add them). */
+typedef struct fpie_batch fpie_batch;
+int fpie_batch_create(double budget_bytes, fpie_batch** out);
+int fpie_batch_destroy(fpie_batch* b);
+/* Device bytes a job of an n x m grid holds (for admission decisions). */
+int fpie_batch_job_bytes(int n, int m, double* bytes);
+/* Copies the job's inputs (host arrays, layouts as fpie_grid_reset); fails
+ * with FPIE_ERR_STATE when the budget has no room.  *job_id receives the
+ * slot, reused after fpie_batch_remove. */
+int fpie_batch_add(fpie_batch* b, int n, int m, const int32_t* mask,
+                   const float* tgt, const float* grad, int iterations,
+                   int* job_id);
+int fpie_batch_run(fpie_batch* b, int max_sweeps);
+int fpie_batch_progress(fpie_batch* b, int job, int* done, int* total);
+/* Clipped uint8 image [n][m][3] and per-channel sum |residual| of a job. */
+int fpie_batch_result(fpie_batch* b, int job, uint8_t* img, float* err);
+int fpie_batch_state(fpie_batch* b, int job, float* out);
+/* FP64 residual norms of `count` jobs: out[6k..6k+2] = max |r| per channel,
+ * out[6k+3..6k+5] = sum |r|, for jobs[k]'s current state. */
+int fpie_batch_norms(fpie_batch* b, const int* jobs, int count, double* out);
+int fpie_batch_remove(fpie_batch* b, int job);
+int fpie_batch_memory(fpie_batch* b, double* used, double* budget);
+/* "auto" or a variant name ("p16w8k16", "p8w16k16", "p16w8k8"). */
+int fpie_batch_set_kernel(fpie_batch* b, const char* name);
+int fpie_batch_kernel(fpie_batch* b, char* buf, int len);
+/* Iterations (about 128 ns each) a CTA may wait for a dependency. */
+int fpie_batch_set_spin_limit(fpie_batch* b, long long spins);
+int fpie_batch_launch_count(fpie_batch* b, long long* count);
 
 /* Kernel launches this solver has issued since creation (sweeps, residual,
  * image, conversions), counted on the host. */

@@ -126,7 +126,8 @@ def test_tensor_handoff(backend):
 
 
 KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16", "r16w10k8s",
-           "r16w12k8s", "r12w16k16s", "p16w8k8", "p16w8k16", "p8w16k16", "p12w10k16", "p8w12k8"]
+           "r16w12k8s", "r12w16k16s", "p16w8k8", "p16w8k16", "p8w16k16", "p8w12k8",
+           "p16w8k4", "p12w12k8s", "p8w16k8s"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)

@@ -1,0 +1,69 @@
+"""Serving loop on the GPU: each result is the same alone and in the mix."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    from fpie_gb300.serve import make_requests
+
+    return make_requests(6, seed=3, max_box=160)
+
+
+def _serve(reqs, **kw):
+    from fpie_gb300.serve import Server
+
+    srv = Server(**kw)
+    for r in reqs:
+        srv.submit(r)
+    t = iter(range(10**9))
+    srv.drain(lambda: float(next(t)))
+    return {r.rid: r for r in srv.finished}, srv
+
+
+def test_alone_equals_in_the_mix():
+    kw = dict(budget_bytes=4e9, epoch_sweeps=128, tol=1e-3, max_sweeps=3000)
+    mixed, _ = _serve(_requests(), **kw)
+    assert len(mixed) == 6
+    for rid in range(6):
+        alone, _ = _serve([_requests()[rid]], **kw)
+        a, b = alone[rid], mixed[rid]
+        assert a.sweeps == b.sweeps
+        np.testing.assert_array_equal(a.img, b.img)
+        np.testing.assert_array_equal(a.err, b.err)
+
+
+def test_results_match_grid_solver_and_stop_rule():
+    from fpie_gb300 import backend
+
+    res, srv = _serve(_requests(), budget_bytes=4e9, epoch_sweeps=128, tol=1e-3, max_sweeps=3000)
+    for rid, r in res.items():
+        assert r.max_residual <= 1e-3 or r.sweeps == 3000
+        assert r.sweeps % 128 == 0 or r.sweeps == 3000
+        s = backend.GridSolver(8, 8)
+        s.reset(r.mask.size, r.mask, r.tgt, r.grad)
+        img, err = s.step(r.sweeps)
+        np.testing.assert_array_equal(r.img, img)
+
+
+def test_budget_limits_concurrency():
+    from fpie_gb300.batch import BatchSolver
+
+    reqs = _requests()
+    biggest = max(BatchSolver.job_bytes(*r.mask.shape) for r in reqs)
+    res, srv = _serve(reqs, budget_bytes=2.2 * biggest, epoch_sweeps=256, tol=1e-2, max_sweeps=2000)
+    assert len(res) == 6 and srv.peak_active <= 2
+
+
+def test_poisson_replay_reports_latency_percentiles():
+    from fpie_gb300.serve import run_workload
+
+    stats = run_workload(_requests(), rate=200.0, budget_bytes=4e9, epoch_sweeps=256, tol=1e-2,
+                         max_sweeps=2000)
+    assert stats["requests"] == 6
+    lat = stats["latency_ms"]
+    assert 0 < lat["p50"] <= lat["p95"] <= lat["p99"] <= lat["max"]
