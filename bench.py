@@ -39,6 +39,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -59,6 +61,11 @@ def parse_args():
     p.add_argument("--no-equ", action="store_true")
     p.add_argument("--kernel", default="auto",
                    help="grid sweep kernel ('auto' = autotuned; a name pins one, e.g. for profiling)")
+    p.add_argument("--workload", choices=["square800", "batch", "serve"], default="square800",
+                   help="square800 (default, the headline line); batch: 256 uneven jobs in one "
+                        "persistent launch vs one GridSolver per job; serve: Poisson arrivals")
+    p.add_argument("--jobs", type=int, default=256)
+    p.add_argument("--rates", default="50,200,500,1000,2000")
     return p.parse_args()
 
 
@@ -399,10 +406,90 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    """256 uneven paste jobs (boxes log-uniform 32..1024, 2000-10000 sweeps each):
+    one persistent batched launch vs the same jobs run one at a time."""
+    import torch
+
+    from fpie_gb300 import backend, prep, workloads
+    from fpie_gb300.batch import BatchSolver
+
+    jobs = []
+    for pb in workloads.job_mix(n_jobs=args.jobs, seed=7):
+        mc, t, g, _ = prep.grid_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt,
+                                       pb.gradient)
+        jobs.append((mc, t, g, pb.iterations))
+    work = sum(int((mc != 0).sum()) * it for mc, t, g, it in jobs)
+    crop_px = sum(mc.size for mc, *_ in jobs)
+    b = BatchSolver(40e9)
+    ids = [b.add(mc, t, g, it) for mc, t, g, it in jobs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run()
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - t0
+    launches = b.launches
+    # The same jobs, one GridSolver each (autotuned per shape), back to back.
+    t0 = time.perf_counter()
+    for mc, t, g, it in jobs:
+        s = backend.GridSolver(8, 8)
+        s.reset(mc.size, mc, t, g)
+        s.sweeps(it)
+        s.sync()
+        s.close()
+    seq_s = time.perf_counter() - t0
+    # spot parity: three jobs against a GridSolver run
+    same = True
+    for k in (0, len(jobs) // 2, len(jobs) - 1):
+        mc, t, g, it = jobs[k]
+        s = backend.GridSolver(8, 8)
+        s.reset(mc.size, mc, t, g)
+        s.step(it)
+        same &= bool(np.array_equal(s.state(), b.state(ids[k])))
+    line = {"metric": "pixel-updates/s", "value": work / batch_s, "unit": "pixel-updates/s",
+            "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": batch_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"{len(jobs)} paste jobs, boxes log-uniform 32..1024, circles/"
+                                   "squares/blobs, src|max gradient, 2000-10000 sweeps each",
+                       "unknown_sweeps": work, "crop_pixels": crop_px,
+                       "batch_kernel": b.kernel, "includes_autotuning": True},
+            "sequential_gridsolver": {"value": work / seq_s, "seconds": seq_s},
+            "batched_seconds": batch_s, "speedup_vs_sequential": seq_s / batch_s,
+            "gpu_launches": launches, "parity_spot_check": same}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Poisson arrivals of the batched-job distribution; each job stops at a
+    max residual of 1e-3 per channel or 10000 sweeps; 40 GB HBM budget."""
+    from fpie_gb300.serve import make_requests, run_workload
+
+    out = {}
+    for rate in [float(r) for r in args.rates.split(",")]:
+        reqs = make_requests(args.jobs, seed=11)
+        out[str(int(rate))] = run_workload(reqs, rate, seed=int(rate), budget_bytes=40e9,
+                                           epoch_sweeps=256, tol=1e-3, max_sweeps=10000)
+        print(json.dumps({"rate": rate, **out[str(int(rate))]}), flush=True)
+    best = max(out.values(), key=lambda r: r["throughput_req_per_s"])
+    line = {"metric": "p99 latency ms (and throughput)", "value": best["latency_ms"]["p99"],
+            "unit": "ms", "higher_is_better": False, "n_gpus": 1, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"serving: {args.jobs} requests per rate, Poisson arrivals, "
+                                   "stop at max|r| <= 1e-3 or 10000 sweeps, 40 GB budget, "
+                                   "256-sweep epochs"},
+            "rates": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gb300(args)
 

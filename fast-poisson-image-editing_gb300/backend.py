@@ -183,6 +183,43 @@ class GridSolver(_Solver):
         _abi.call("fpie_grid_kernel", self._h, buf, 64)
         return buf.value.decode()
 
+    def reset_images(self, src, mask, tgt, mask_on_src: tuple[int, int],
+                     mask_on_tgt: tuple[int, int], gradient: str = "max") -> tuple[int, int, int, int]:
+        """Build the inputs on the GPU from uint8 images (GridProcessor.reset semantics).
+
+        Arrays may be numpy (copied to the device) or torch CUDA uint8 tensors.
+        Returns the crop on the target (row0, row1, col0, col1).
+        """
+        mode = {"src": 0, "avg": 1, "max": 2}.get(gradient)
+        if mode is None:
+            raise _abi.FpieArgumentError(f"unknown gradient mode {gradient!r}")
+        on_dev = bool(getattr(src, "is_cuda", False))
+        if on_dev:
+            arrs = [_tensor_ptr(a, "uint8", n) for a, n in ((src, "src"), (mask, "mask"), (tgt, "tgt"))]
+            shapes = [tuple(a.shape) for a in (src, mask, tgt)]
+        else:
+            keep = [np.ascontiguousarray(a, dtype=np.uint8) for a in (src, mask, tgt)]
+            arrs = [_ptr(a) for a in keep]
+            shapes = [a.shape for a in keep]
+        (sh, sw, sc), msh, (th, tw, tc) = shapes
+        if sc != 3 or tc != 3 or len(msh) not in (2, 3):
+            raise _abi.FpieArgumentError("src/tgt must be HxWx3 and the mask HxW or HxWx3")
+        mch = 1 if len(msh) == 2 else msh[2]
+        box = (ctypes.c_int * 4)()
+        _abi.call("fpie_grid_reset_images", self._h, arrs[0], sh, sw, arrs[1], msh[0], msh[1], mch,
+                  arrs[2], th, tw, int(mask_on_src[0]), int(mask_on_src[1]), int(mask_on_tgt[0]),
+                  int(mask_on_tgt[1]), mode, 1 if on_dev else 0, box)
+        self.shape = (box[1] - box[0], box[3] - box[2])
+        self.N = self.shape[0] * self.shape[1]
+        return tuple(box)
+
+    def inputs(self) -> tuple[np.ndarray, np.ndarray]:
+        """(mask int32[n,m], grad float32[n,m,3]) as the solver holds them."""
+        mask = np.empty(self.shape, np.int32)
+        grad = np.empty((*self.shape, 3), np.float32)
+        _abi.call("fpie_grid_get_inputs", self._h, _ptr(mask), _ptr(grad))
+        return mask, grad
+
     def residual_norms(self) -> tuple[np.ndarray, np.ndarray]:
         """(max |r| per channel, sum |r| per channel) of the current state, FP64."""
         out = np.empty(6, np.float64)

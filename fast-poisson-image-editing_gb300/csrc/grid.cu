@@ -22,6 +22,36 @@
 
 namespace fpie {
 
+struct PrepArgs {
+  GridGeom G;
+  const uint8_t* m01;
+  int mw, x0, y0;
+  const uint8_t* src;
+  int sw, sx, sy;
+  const uint8_t* tgt;
+  int tw, tx, ty;
+  int mode;
+};
+void launch_prep_mask(const uint8_t* mask, int mh, int mw, int mch, uint8_t* m01, int* box,
+                      cudaStream_t st);
+void launch_prep_grid(const PrepArgs& a, uint8_t* mask, float* xa, float* xb, float* g,
+                      cudaStream_t st);
+
+__global__ void grid_inputs_unpack_kernel(GridGeom G, const uint8_t* __restrict__ mask,
+                                          const float* __restrict__ g,
+                                          int32_t* __restrict__ mask_out,
+                                          float* __restrict__ grad_out) {
+  const long long total = (long long)G.n * G.m;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / G.m), j = (int)(idx % G.m);
+    const long long p = G.at(i, j);
+    mask_out[idx] = mask[p];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) grad_out[idx * 3 + c] = g[c * G.plane + p];
+  }
+}
+
 // ---- layout conversion kernels ------------------------------------------------
 
 __global__ void grid_pack_kernel(GridGeom G, const int32_t* __restrict__ mk,
@@ -79,6 +109,7 @@ struct GridSolverImpl : Solver {
   float* d_err = nullptr;
   uint8_t* h_img = nullptr;
   float* h_err = nullptr;
+  int* h_box = nullptr;  // pinned, for the GPU-side reset's bounding box
   GridLaunch L{};
   static constexpr int kChunk = 64;  // sweeps per captured graph (even)
   cudaGraphExec_t chunk[2] = {nullptr, nullptr};
@@ -110,6 +141,7 @@ struct GridSolverImpl : Solver {
     release();
     if (h_err) cudaFreeHost(h_err);
     if (h_norm) cudaFreeHost(h_norm);
+    if (h_box) cudaFreeHost(h_box);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -235,6 +267,89 @@ struct GridSolverImpl : Solver {
     allocate(n, m);
     N_user = n * m;
     pack(dm, dt, dg);
+  }
+
+  // Builds the solver inputs on the GPU from the three uint8 images
+  // (prep.cu), the device counterpart of GridProcessor.reset.  box_out
+  // receives the crop on the target (row0, row1, col0, col1).
+  void reset_images(const uint8_t* src, int sh, int sw, const uint8_t* msk, int mh, int mw,
+                    int mch, const uint8_t* tgt, int th, int tw, int s_row, int s_col,
+                    int t_row, int t_col, int mode, bool on_device, int* box_out) {
+    FPIE_REQUIRE(src && msk && tgt && box_out, FPIE_ERR_ARG, "null input array");
+    FPIE_REQUIRE(sh > 0 && sw > 0 && mh > 0 && mw > 0 && th > 0 && tw > 0, FPIE_ERR_ARG,
+                 "empty image");
+    FPIE_REQUIRE(mch == 1 || mch == 3, FPIE_ERR_ARG, "mask must have 1 or 3 channels");
+    FPIE_REQUIRE(mode >= 0 && mode <= 2, FPIE_ERR_ARG,
+                 "gradient mode must be 0 (src), 1 (avg), 2 (max)");
+    const size_t sb = (size_t)sh * sw * 3, mb = (size_t)mh * mw * mch, tb = (size_t)th * tw * 3;
+    const size_t mpx = (size_t)mh * mw;
+    char* stage = nullptr;
+    const size_t head = on_device ? 0 : (sb + mb + tb + 15) / 16 * 16;
+    FPIE_CUDA(cudaMallocAsync(&stage, head + 16 + mpx, stream));
+    const uint8_t *dsrc = src, *dmsk = msk, *dtgt = tgt;
+    if (!on_device) {
+      FPIE_CUDA(cudaMemcpyAsync(stage, src, sb, cudaMemcpyHostToDevice, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage + sb, msk, mb, cudaMemcpyHostToDevice, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage + sb + mb, tgt, tb, cudaMemcpyHostToDevice, stream));
+      dsrc = reinterpret_cast<uint8_t*>(stage);
+      dmsk = reinterpret_cast<uint8_t*>(stage + sb);
+      dtgt = reinterpret_cast<uint8_t*>(stage + sb + mb);
+    }
+    int* dbox = reinterpret_cast<int*>(stage + head);
+    uint8_t* m01 = reinterpret_cast<uint8_t*>(stage + head + 16);
+    if (!h_box) FPIE_CUDA(cudaMallocHost(&h_box, 4 * sizeof(int)));
+    h_box[0] = INT32_MAX;
+    h_box[1] = -1;
+    h_box[2] = INT32_MAX;
+    h_box[3] = -1;
+    FPIE_CUDA(cudaMemcpyAsync(dbox, h_box, 4 * sizeof(int), cudaMemcpyHostToDevice, stream));
+    launch_prep_mask(dmsk, mh, mw, mch, m01, dbox, stream);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(h_box, dbox, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    const int b0 = h_box[0], b1 = h_box[1], b2 = h_box[2], b3 = h_box[3];
+    if (b1 < 0) {
+      cudaFreeAsync(stage, stream);
+      throw Error{FPIE_ERR_ARG, "the mask selects no pixel (after clearing its 1-pixel frame)"};
+    }
+    const int x0 = b0 - 1, x1 = b1 + 2, y0 = b2 - 1, y1 = b3 + 2;
+    const bool fits = s_row + x0 >= 0 && s_col + y0 >= 0 && s_row + x1 <= sh && s_col + y1 <= sw &&
+                      t_row + x0 >= 0 && t_col + y0 >= 0 && t_row + x1 <= th && t_col + y1 <= tw;
+    if (!fits) {
+      cudaFreeAsync(stage, stream);
+      throw Error{FPIE_ERR_ARG,
+                  "the mask's crop at the given offsets leaves the source or target image"};
+    }
+    allocate(x1 - x0, y1 - y0);
+    N_user = G.n * G.m;
+    PrepArgs a{G, m01, mw, x0, y0, dsrc, sw, s_row + x0, s_col + y0, dtgt, tw, t_row + x0,
+               t_col + y0, mode};
+    launch_prep_grid(a, mask, x[0], x[1], g, stream);
+    post_launch(this);
+    FPIE_CUDA(cudaFreeAsync(stage, stream));
+    ready = true;
+    flags_ok = false;
+    mflags_ok = false;
+    box_out[0] = t_row + x0;
+    box_out[1] = t_row + x1;
+    box_out[2] = t_col + y0;
+    box_out[3] = t_col + y1;
+    if (!on_device) FPIE_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  void get_inputs(int32_t* mask_out, float* grad_out) {
+    FPIE_REQUIRE(mask_out && grad_out, FPIE_ERR_ARG, "null output array");
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
+    const long long total = (long long)G.n * G.m;
+    char* tmp = nullptr;
+    FPIE_CUDA(cudaMallocAsync(&tmp, total * 16, stream));
+    grid_inputs_unpack_kernel<<<conv_blocks(total), 256, 0, stream>>>(
+        G, mask, g, reinterpret_cast<int32_t*>(tmp), reinterpret_cast<float*>(tmp + total * 4));
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(mask_out, tmp, total * 4, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaMemcpyAsync(grad_out, tmp + total * 4, total * 12, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaFreeAsync(tmp, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 
   // ---- sweep kernels ---------------------------------------------------------
@@ -693,6 +808,21 @@ int fpie_grid_step(fpie_solver* s, int iteration, uint8_t* img_out,
 int fpie_grid_reset_device(fpie_solver* s, int n, int m, const int32_t* mask,
                            const float* tgt, const float* grad) {
   return guarded([&] { grid_of(s)->reset_device(n, m, mask, tgt, grad); });
+}
+
+int fpie_grid_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int src_w,
+                           const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
+                           const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
+                           int tgt_row, int tgt_col, int gradient, int on_device, int* box) {
+  return guarded([&] {
+    grid_of(s)->reset_images(src, src_h, src_w, mask, mask_h, mask_w, mask_channels, tgt, tgt_h,
+                             tgt_w, src_row, src_col, tgt_row, tgt_col, gradient, on_device != 0,
+                             box);
+  });
+}
+
+int fpie_grid_get_inputs(fpie_solver* s, int32_t* mask_out, float* grad_out) {
+  return guarded([&] { grid_of(s)->get_inputs(mask_out, grad_out); });
 }
 
 int fpie_residual_norms(fpie_solver* s, double* out) {

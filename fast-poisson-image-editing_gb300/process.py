@@ -128,10 +128,19 @@ class GridProcessor(BaseProcessor):
 
     def __init__(self, gradient: str = "max", backend: str = DEFAULT_BACKEND,
                  n_cpu: int = CPU_COUNT, min_interval: int = 100, block_size: int = 1024,
-                 grid_x: int = 8, grid_y: int = 8):
+                 grid_x: int = 8, grid_y: int = 8, device_prep: bool = False):
+        """device_prep: build mask/crop/grad on the GPU from the uint8 images
+        (fpie_grid_reset_images) instead of with numpy on the host."""
         super().__init__(gradient, 0, backend, _make_core("grid", backend, block_size, grid_x, grid_y))
+        self.device_prep = device_prep
 
     def reset(self, src, mask, tgt, mask_on_src, mask_on_tgt) -> int:
+        if self.device_prep:
+            x0, x1, y0, y1 = self.core.reset_images(src, mask, tgt, mask_on_src, mask_on_tgt,
+                                                    self.gradient)
+            self.x0, self.x1, self.y0, self.y1 = x0, x1, y0, y1
+            self.tgt = tgt.copy()
+            return (x1 - x0) * (y1 - y0)
         mc, t, grad, crop = prep.grid_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, self.gradient)
         self.x0, self.x1, self.y0, self.y1 = crop.x0, crop.x1, crop.y0, crop.y1
         self.tgt = tgt.copy()

@@ -126,6 +126,24 @@ int fpie_equ_reset_device(fpie_solver* s, int N, const int32_t* A,
 int fpie_equ_step_device(fpie_solver* s, int iteration, uint8_t* x,
                          float* err);
 
+/* GPU-side counterpart of GridProcessor.reset (fpie/process.py:422-487):
+ * builds the grid inputs from the uint8 images -- src [src_h][src_w][3],
+ * mask [mask_h][mask_w][mask_channels] (1 or 3), tgt [tgt_h][tgt_w][3] --
+ * the mask's placement (src_row, src_col) on the source and (tgt_row,
+ * tgt_col) on the target, and gradient 0 = 'src', 1 = 'avg', 2 = 'max'.
+ * Bit-identical to the host construction.  on_device != 0: the pointers are
+ * device memory (nothing is copied from the host).  box receives the crop on
+ * the target: row0, row1, col0, col1 (end-exclusive).  Errors: a mask with no
+ * set pixel, or a crop leaving either image (FPIE_ERR_ARG). */
+int fpie_grid_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int src_w,
+                           const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
+                           const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
+                           int tgt_row, int tgt_col, int gradient, int on_device, int* box);
+
+/* Copies the grid inputs the solver holds (mask int32[n][m], grad
+ * float32[n][m][3]) to host memory. */
+int fpie_grid_get_inputs(fpie_solver* s, int32_t* mask_out, float* grad_out);
+
 /* Only the sweeps of a step (no residual, no image); for timing the sweep
  * kernels on their own. */
 int fpie_sweeps(fpie_solver* s, int iteration);
