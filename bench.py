@@ -66,6 +66,8 @@ def parse_args():
                         "persistent launch vs one GridSolver per job; serve: Poisson arrivals")
     p.add_argument("--jobs", type=int, default=256)
     p.add_argument("--rates", default="50,200,500,1000,2000")
+    p.add_argument("--precision", choices=["fp32", "fp16", "bf16"], default="fp32",
+                   help="batch/serve workloads: FP32 or a mixed form")
     return p.parse_args()
 
 
@@ -421,7 +423,7 @@ def run_batch(args):
         jobs.append((mc, t, g, pb.iterations))
     work = sum(int((mc != 0).sum()) * it for mc, t, g, it in jobs)
     crop_px = sum(mc.size for mc, *_ in jobs)
-    b = BatchSolver(40e9)
+    b = BatchSolver(40e9, precision=args.precision)
     ids = [b.add(mc, t, g, it) for mc, t, g, it in jobs]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -429,21 +431,26 @@ def run_batch(args):
     torch.cuda.synchronize()
     batch_s = time.perf_counter() - t0
     launches = b.launches
-    # The same jobs, one GridSolver each (autotuned per shape), back to back.
+    # The same jobs, one GridSolver each with the batch's kernel, back to back.
+    def solo(mc, t, g):
+        s = backend.GridSolver(8, 8)
+        s.set_precision(args.precision)
+        s.set_kernel(b.kernel)
+        s.reset(mc.size, mc, t, g)
+        return s
+
     t0 = time.perf_counter()
     for mc, t, g, it in jobs:
-        s = backend.GridSolver(8, 8)
-        s.reset(mc.size, mc, t, g)
+        s = solo(mc, t, g)
         s.sweeps(it)
         s.sync()
         s.close()
     seq_s = time.perf_counter() - t0
-    # spot parity: three jobs against a GridSolver run
+    # spot parity: three jobs against a GridSolver run of the same kernel
     same = True
     for k in (0, len(jobs) // 2, len(jobs) - 1):
         mc, t, g, it = jobs[k]
-        s = backend.GridSolver(8, 8)
-        s.reset(mc.size, mc, t, g)
+        s = solo(mc, t, g)
         s.step(it)
         same &= bool(np.array_equal(s.state(), b.state(ids[k])))
     line = {"metric": "pixel-updates/s", "value": work / batch_s, "unit": "pixel-updates/s",
@@ -452,6 +459,7 @@ def run_batch(args):
             "data": "synthetic",
             "config": {"workload": f"{len(jobs)} paste jobs, boxes log-uniform 32..1024, circles/"
                                    "squares/blobs, src|max gradient, 2000-10000 sweeps each",
+                       "precision": args.precision,
                        "unknown_sweeps": work, "crop_pixels": crop_px,
                        "batch_kernel": b.kernel, "includes_autotuning": True},
             "sequential_gridsolver": {"value": work / seq_s, "seconds": seq_s},
@@ -469,7 +477,8 @@ def run_serve(args):
     for rate in [float(r) for r in args.rates.split(",")]:
         reqs = make_requests(args.jobs, seed=11)
         out[str(int(rate))] = run_workload(reqs, rate, seed=int(rate), budget_bytes=40e9,
-                                           epoch_sweeps=256, tol=1e-3, max_sweeps=10000)
+                                           epoch_sweeps=256, tol=1e-3, max_sweeps=10000,
+                                           precision=args.precision)
         print(json.dumps({"rate": rate, **out[str(int(rate))]}), flush=True)
     best = max(out.values(), key=lambda r: r["throughput_req_per_s"])
     line = {"metric": "p99 latency ms (and throughput)", "value": best["latency_ms"]["p99"],
@@ -477,7 +486,7 @@ def run_serve(args):
             "data": "synthetic",
             "config": {"workload": f"serving: {args.jobs} requests per rate, Poisson arrivals, "
                                    "stop at max|r| <= 1e-3 or 10000 sweeps, 40 GB budget, "
-                                   "256-sweep epochs"},
+                                   "256-sweep epochs", "precision": args.precision},
             "rates": out}
     print(json.dumps(line), flush=True)
 

@@ -66,6 +66,8 @@ _PROTOS: dict[str, tuple] = {
     "fpie_batch_create": ([ctypes.c_double, ctypes.POINTER(_P)], _I),
     "fpie_batch_destroy": ([_P], _I),
     "fpie_batch_job_bytes": ([_I, _I, ctypes.POINTER(ctypes.c_double)], _I),
+    "fpie_batch_job_bytes_for": ([_P, _I, _I, ctypes.POINTER(ctypes.c_double)], _I),
+    "fpie_batch_set_precision": ([_P, _I], _I),
     "fpie_batch_add": ([_P, _I, _I, _P, _P, _P, _I, ctypes.POINTER(_I)], _I),
     "fpie_batch_run": ([_P, _I], _I),
     "fpie_batch_progress": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),

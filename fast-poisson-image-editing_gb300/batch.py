@@ -18,11 +18,23 @@ from .backend import _as, _ptr
 
 
 class BatchSolver:
-    def __init__(self, budget_bytes: float = 40e9) -> None:
+    def __init__(self, budget_bytes: float = 40e9, precision: str = "fp32") -> None:
+        from .backend import PRECISIONS
+
         self._lib = _abi.lib()
         self._h = ctypes.c_void_p()
         _abi.call("fpie_batch_create", float(budget_bytes), ctypes.byref(self._h))
+        if precision not in PRECISIONS:
+            raise _abi.FpieArgumentError(f"unknown precision {precision!r}")
+        _abi.call("fpie_batch_set_precision", self._h, PRECISIONS[precision])
+        self.precision = precision
         self._shape: dict[int, tuple[int, int]] = {}
+
+    def job_bytes_for(self, n: int, m: int) -> int:
+        """Device bytes a job of an n x m grid takes in this batch's precision."""
+        b = ctypes.c_double(0)
+        _abi.call("fpie_batch_job_bytes_for", self._h, int(n), int(m), ctypes.byref(b))
+        return int(b.value)
 
     def __del__(self) -> None:
         h = getattr(self, "_h", None)

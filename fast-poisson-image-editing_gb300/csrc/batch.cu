@@ -21,6 +21,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -35,12 +36,100 @@ struct BJobDev {
   const uint8_t* mask;
   const float* g;
   float* x[2];
+  void* e[2];       // mixed forms: the correction (FP16 / BF16 planes)
+  float* r;         // mixed forms: the FP32 residual planes
   int tiles_x;      // tiles per row of this job
   int ntiles;       // active tiles
   int tile_off;     // first entry of this job in the tile list
   int sweeps;       // sweeps in this launch
   int parity;       // buffer holding the state at level 0
 };
+
+// Level schedule of the mixed forms for a launch of S sweeps with depth K:
+// level 0 computes the residual of x; then every cycle of up to 64 sweeps
+// has ceil(len/K) inner levels on the correction (the first starting from
+// 0) and one fold level (x += e into the other x buffer, new residual).
+struct MixedLevel {
+  int type;    // 0 = residual, 1 = inner, 2 = fold
+  int k;       // inner: sweeps
+  int pos;     // inner: index within the cycle (0 = zero start)
+  int cycle;   // fold / inner: cycle index (x parity offset)
+  int ninner;  // inner levels of this cycle
+};
+
+__host__ __device__ inline int mixed_levels(int S, int K) {
+  const int P = 64 / K, C = S / 64, rem = S % 64;
+  return 1 + C * (P + 1) + (rem ? (rem + K - 1) / K + 1 : 0);
+}
+
+__host__ __device__ inline MixedLevel mixed_level(int z, int S, int K) {
+  MixedLevel L{0, 0, 0, 0, 0};
+  if (z == 0) return L;
+  const int P = 64 / K, C = S / 64, rem = S % 64;
+  int zz = z - 1, cyc = zz / (P + 1), pos = zz % (P + 1), len = 64, ninner = P;
+  if (cyc >= C) {  // the last, partial cycle
+    cyc = C;
+    pos = zz - C * (P + 1);
+    len = rem;
+    ninner = (rem + K - 1) / K;
+  }
+  L.cycle = cyc;
+  L.ninner = ninner;
+  if (pos < ninner) {
+    L.type = 1;
+    L.pos = pos;
+    L.k = len - pos * K < K ? len - pos * K : K;
+  } else {
+    L.type = 2;
+  }
+  return L;
+}
+
+template <typename TS>
+__device__ __forceinline__ float4 ld4cg_any(const TS* p) {
+  return Lanes4<TS, true>::load(p);
+}
+
+// One channel of one tile interior: optional fold x_out = x_in + e, then
+// the FP32 residual r = g + sum(neighbours) - 4x of the (folded) state.
+// Reads go through L2 (other CTAs wrote x and e in this launch).
+template <typename TS>
+__device__ void refine_tile(const GridGeom& G, const uint8_t* __restrict__ mask,
+                            const float* __restrict__ gc, const float* xin, const TS* e,
+                            float* xout, float* r, int r0, int c0, int th, int tw) {
+  const int gpr = tw / 4;
+  for (int q = threadIdx.x; q < th * gpr; q += blockDim.x) {
+    const int i = r0 + q / gpr, j = c0 + 4 * (q % gpr);
+    if (i >= G.n || j >= G.m) continue;
+    const long long p = G.at(i, j);
+    const uint32_t mk = *reinterpret_cast<const uint32_t*>(mask + p);
+    float4 ce = __ldcg(reinterpret_cast<const float4*>(xin + p));
+    float4 up = __ldcg(reinterpret_cast<const float4*>(xin + p - G.pitch));
+    float4 dn = __ldcg(reinterpret_cast<const float4*>(xin + p + G.pitch));
+    float lf = __ldcg(xin + p - 1), rt = __ldcg(xin + p + 4);
+    if (e) {
+      const float4 ec = ld4cg_any(e + p), eu = ld4cg_any(e + p - G.pitch), ed = ld4cg_any(e + p + G.pitch);
+      const float4 el = ld4cg_any(e + p - 4), er = ld4cg_any(e + p + 4);
+      ce = make_float4(__fadd_rn(ce.x, ec.x), __fadd_rn(ce.y, ec.y), __fadd_rn(ce.z, ec.z), __fadd_rn(ce.w, ec.w));
+      up = make_float4(__fadd_rn(up.x, eu.x), __fadd_rn(up.y, eu.y), __fadd_rn(up.z, eu.z), __fadd_rn(up.w, eu.w));
+      dn = make_float4(__fadd_rn(dn.x, ed.x), __fadd_rn(dn.y, ed.y), __fadd_rn(dn.z, ed.z), __fadd_rn(dn.w, ed.w));
+      lf = __fadd_rn(lf, el.w);
+      rt = __fadd_rn(rt, er.x);
+      if (mk) *reinterpret_cast<float4*>(xout + p) = ce;
+    }
+    const float4 gv = __ldg(reinterpret_cast<const float4*>(gc + p));
+    const float xv[6] = {lf, ce.x, ce.y, ce.z, ce.w, rt};
+    const float g4[4] = {gv.x, gv.y, gv.z, gv.w}, u4[4] = {up.x, up.y, up.z, up.w},
+                d4[4] = {dn.x, dn.y, dn.z, dn.w};
+    float rr[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool on = (mk >> (8 * k)) & 0xffu;
+      rr[k] = on ? -grid_res(xv[k + 1], g4[k], u4[k], d4[k], xv[k], xv[k + 2]) : 0.0f;
+    }
+    *reinterpret_cast<float4*>(r + p) = make_float4(rr[0], rr[1], rr[2], rr[3]);
+  }
+}
 
 struct BQueue {
   const BJobDev* jobs;
@@ -66,9 +155,10 @@ __device__ __forceinline__ int upper_bound_idx(const T* a, int n, T v) {
   return lo;
 }
 
-template <int R, int W, int K>
+template <int R, int W, int K, typename TS>
 __global__ void __launch_bounds__(W * 32)
 batch_persistent_kernel(BQueue Q) {
+  constexpr bool MIXED = !std::is_same<TS, float>::value;
   constexpr int TH = W * R - 2 * K;
   constexpr int TW = 128 - 2 * K;
   __shared__ float4 edge[2][2][W][32];
@@ -109,15 +199,43 @@ batch_persistent_kernel(BQueue Q) {
     const int2 tf = Q.tiles[J.tile_off + ti];
     const int ty = tf.x / J.tiles_x, tx = tf.x - ty * J.tiles_x;
     const long long base = J.G.at(ty * TH - K + w * R, tx * TW - K + 4 * lane);
-    const int pin = (J.parity + z) & 1;
-    const float* xc = J.x[pin] + c * J.G.plane;
-    float* oc = J.x[pin ^ 1] + c * J.G.plane;
-    const float* gc = J.g + c * J.G.plane;
-    const int ks = min(K, J.sweeps - z * K);
-    if (tf.y == 2)
-      tbp_body<R, W, K, true, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
-    else
-      tbp_body<R, W, K, false, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+    const long long co = c * J.G.plane;
+    const float* gc = J.g + co;
+    if (!MIXED) {
+      const int pin = (J.parity + z) & 1;
+      const float* xc = J.x[pin] + co;
+      float* oc = J.x[pin ^ 1] + co;
+      const int ks = min(K, J.sweeps - z * K);
+      if (tf.y == 2)
+        tbp_body<R, W, K, true, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+      else
+        tbp_body<R, W, K, false, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+    } else {
+      const MixedLevel L = mixed_level(z, J.sweeps, K);
+      const int xp = (J.parity + L.cycle) & 1;
+      TS* e0 = static_cast<TS*>(J.e[0]);
+      TS* e1 = static_cast<TS*>(J.e[1]);
+      if (L.type == 1) {
+        const TS* ein = ((L.pos - 1) & 1) ? e1 : e0;
+        TS* eout = (L.pos & 1) ? e1 : e0;
+        const float* rc = J.r + co;
+        if (L.pos == 0) {
+          if (tf.y == 2)
+            tbp_body<R, W, K, true, TS, true, true>(J.G, J.mask, rc, nullptr, eout + co, base, L.k, lane, w, edge);
+          else
+            tbp_body<R, W, K, false, TS, true, true>(J.G, J.mask, rc, nullptr, eout + co, base, L.k, lane, w, edge);
+        } else {
+          if (tf.y == 2)
+            tbp_body<R, W, K, true, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
+          else
+            tbp_body<R, W, K, false, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
+        }
+      } else {
+        const TS* elast = L.type == 2 ? (((L.ninner - 1) & 1) ? e1 : e0) + co : nullptr;
+        refine_tile<TS>(J.G, J.mask, gc, J.x[xp] + co, elast, J.x[xp ^ 1] + co, J.r + co,
+                        ty * TH, tx * TW, TH, TW);
+      }
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) atomicAdd(Q.done + j, 1);
@@ -127,19 +245,23 @@ batch_persistent_kernel(BQueue Q) {
 struct BatchVariant {
   const char* name;
   int rows, warps, depth, tile_h, tile_w;
-  const void* kernel;
-  void (*launch)(int grid, const BQueue& q, cudaStream_t st);
+  const void* kernel[3];  // by precision: FP32, mixed FP16, mixed BF16
+  void (*launch[3])(int grid, const BQueue& q, cudaStream_t st);
 };
 
-template <int R, int W, int K>
+template <int R, int W, int K, typename TS>
 void launch_batch(int grid, const BQueue& q, cudaStream_t st) {
-  batch_persistent_kernel<R, W, K><<<grid, W * 32, 0, st>>>(q);
+  batch_persistent_kernel<R, W, K, TS><<<grid, W * 32, 0, st>>>(q);
 }
 
 template <int R, int W, int K>
 BatchVariant make_bv(const char* name) {
   return BatchVariant{name, R, W, K, W * R - 2 * K, 128 - 2 * K,
-                      (const void*)&batch_persistent_kernel<R, W, K>, &launch_batch<R, W, K>};
+                      {(const void*)&batch_persistent_kernel<R, W, K, float>,
+                       (const void*)&batch_persistent_kernel<R, W, K, __half>,
+                       (const void*)&batch_persistent_kernel<R, W, K, __nv_bfloat16>},
+                      {&launch_batch<R, W, K, float>, &launch_batch<R, W, K, __half>,
+                       &launch_batch<R, W, K, __nv_bfloat16>}};
 }
 
 static const std::vector<BatchVariant>& batch_variants() {
@@ -158,6 +280,10 @@ struct BatchJob {
   GridGeom G{};
   GridLaunch L{};
   std::vector<uint8_t> hmask;  // 0/1 crop mask, for tile lists
+  // Active-tile lists per batch variant, built on first use (the mask of a
+  // job never changes).
+  std::vector<std::vector<int2>> tiles_of;
+  std::vector<int> tiles_x_of;
   float* x[2] = {nullptr, nullptr};
   float* g = nullptr;
   uint8_t* mask = nullptr;
@@ -165,6 +291,8 @@ struct BatchJob {
   double* parts = nullptr;  // per-block partials: 6 doubles each (norms need 6)
   float* err = nullptr;
   double* norm = nullptr;   // [max|r| x3, sum|r| x3] of the last norms() call
+  void* e[2] = {nullptr, nullptr};  // mixed forms only
+  float* r = nullptr;               // mixed forms only
   int cur = 0;
   int sweeps_total = 0, sweeps_done = 0;
   bool live = false;
@@ -212,10 +340,13 @@ struct Batch {
     cudaStreamDestroy(stream);
   }
 
-  static size_t job_bytes(int n, int m) {
+  int precision = FPIE_FP32;
+
+  static size_t job_bytes(int n, int m, int precision = FPIE_FP32) {
     const GridGeom G = make_geom(n, m);
     const GridLaunch L = grid_launch(G);
-    return (size_t)G.plane * (9 * sizeof(float) + 1) + (size_t)n * m * 3 +
+    const size_t mixed = precision == FPIE_FP32 ? 0 : (size_t)G.plane * 3 * (2 * 2 + 4);
+    return mixed + (size_t)G.plane * (9 * sizeof(float) + 1) + (size_t)n * m * 3 +
            (size_t)L.nparts * 6 * sizeof(double) + 3 * sizeof(float) + 6 * sizeof(double) +
            7 * 256;
   }
@@ -229,6 +360,11 @@ struct Batch {
     cudaFree(j.parts);
     cudaFree(j.err);
     cudaFree(j.norm);
+    cudaFree(j.e[0]);
+    cudaFree(j.e[1]);
+    cudaFree(j.r);
+    j.e[0] = j.e[1] = nullptr;
+    j.r = nullptr;
     j.x[0] = j.x[1] = j.g = nullptr;
     j.mask = j.img = nullptr;
     j.parts = nullptr;
@@ -242,7 +378,7 @@ struct Batch {
     FPIE_REQUIRE(n >= 1 && m >= 1 && hm && ht && hg, FPIE_ERR_ARG, "bad job arrays");
     FPIE_REQUIRE(iterations >= 0, FPIE_ERR_ARG, "negative sweep count");
     FPIE_REQUIRE((long long)n * m <= (1LL << 29), FPIE_ERR_ARG, "job too large");
-    const size_t need = job_bytes(n, m);
+    const size_t need = job_bytes(n, m, precision);
     FPIE_REQUIRE(used + need <= budget, FPIE_ERR_STATE,
                  "job needs " + std::to_string(need) + " bytes; HBM budget left is " +
                      std::to_string(budget - used));
@@ -270,6 +406,15 @@ struct Batch {
       FPIE_CUDA(cudaMalloc(&j.parts, (size_t)j.L.nparts * 6 * sizeof(double)));
       FPIE_CUDA(cudaMalloc(&j.err, 3 * sizeof(float)));
       FPIE_CUDA(cudaMalloc(&j.norm, 6 * sizeof(double)));
+      if (precision != FPIE_FP32) {
+        const size_t eb = (size_t)j.G.plane * 3 * 2, rb = (size_t)j.G.plane * 3 * sizeof(float);
+        FPIE_CUDA(cudaMalloc(&j.e[0], eb));
+        FPIE_CUDA(cudaMalloc(&j.e[1], eb));
+        FPIE_CUDA(cudaMalloc(&j.r, rb));
+        FPIE_CUDA(cudaMemsetAsync(j.e[0], 0, eb, stream));
+        FPIE_CUDA(cudaMemsetAsync(j.e[1], 0, eb, stream));
+        FPIE_CUDA(cudaMemsetAsync(j.r, 0, rb, stream));
+      }
       FPIE_CUDA(cudaMemsetAsync(j.x[0], 0, 3 * pb, stream));
       FPIE_CUDA(cudaMemsetAsync(j.x[1], 0, 3 * pb, stream));
       FPIE_CUDA(cudaMemsetAsync(j.g, 0, 3 * pb, stream));
@@ -330,18 +475,26 @@ struct Batch {
   float launch(const std::vector<int>& ids, const std::vector<int>& sw, int vi, bool time_it) {
     const BatchVariant& v = batch_variants()[vi];
     std::vector<BJobDev> dj;
-    std::vector<int2> tiles, tl;
+    std::vector<int2> tiles;
     std::vector<int> levels;
     for (size_t k = 0; k < ids.size(); ++k) {
       BatchJob& j = jobs[ids[k]];
-      int tx = 0;
-      tile_list(j, v, tl, tx);
+      if (j.tiles_of.size() != batch_variants().size()) {
+        j.tiles_of.assign(batch_variants().size(), {});
+        j.tiles_x_of.assign(batch_variants().size(), -1);
+      }
+      if (j.tiles_x_of[vi] < 0) tile_list(j, v, j.tiles_of[vi], j.tiles_x_of[vi]);
+      const std::vector<int2>& tl = j.tiles_of[vi];
+      const int tx = j.tiles_x_of[vi];
       BJobDev d;
       d.G = j.G;
       d.mask = j.mask;
       d.g = j.g;
       d.x[0] = j.x[0];
       d.x[1] = j.x[1];
+      d.e[0] = j.e[0];
+      d.e[1] = j.e[1];
+      d.r = j.r;
       d.tiles_x = tx;
       d.ntiles = (int)tl.size();
       d.tile_off = (int)tiles.size();
@@ -349,7 +502,9 @@ struct Batch {
       d.parity = j.cur;
       tiles.insert(tiles.end(), tl.begin(), tl.end());
       dj.push_back(d);
-      levels.push_back(d.ntiles > 0 ? (sw[k] + v.depth - 1) / v.depth : 0);
+      const int lv = precision == FPIE_FP32 ? (sw[k] + v.depth - 1) / v.depth
+                                            : (sw[k] > 0 ? mixed_levels(sw[k], v.depth) : 0);
+      levels.push_back(d.ntiles > 0 ? lv : 0);
     }
     const int nj = (int)dj.size();
     std::vector<int> order(nj);
@@ -401,7 +556,8 @@ struct Batch {
       q.spin_limit = spin_limit;
       FPIE_CUDA(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, stream));
       int occ = 0;
-      FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v.kernel, v.warps * 32, 0));
+      FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v.kernel[precision],
+                                                              v.warps * 32, 0));
       const int grid = std::max(1, occ) * sms;
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (time_it) {
@@ -409,7 +565,7 @@ struct Batch {
         FPIE_CUDA(cudaEventCreate(&e1));
         FPIE_CUDA(cudaEventRecord(e0, stream));
       }
-      v.launch(grid, q, stream);
+      v.launch[precision](grid, q, stream);
       FPIE_CUDA(cudaGetLastError());
       ++launches;
       if (time_it) FPIE_CUDA(cudaEventRecord(e1, stream));
@@ -427,7 +583,11 @@ struct Batch {
     }
     for (size_t k = 0; k < ids.size(); ++k) {
       BatchJob& j = jobs[ids[k]];
-      if (levels[k] & 1) j.cur ^= 1;
+      if (levels[k] > 0) {
+        // FP32: one buffer flip per level; mixed: one per fold level.
+        const int flips = precision == FPIE_FP32 ? levels[k] : (sw[k] + 63) / 64;
+        if (flips & 1) j.cur ^= 1;
+      }
       j.sweeps_done += sw[k];
     }
     return ms;
@@ -568,6 +728,24 @@ int fpie_batch_job_bytes(int n, int m, double* bytes) {
   return guarded([&] {
     FPIE_REQUIRE(bytes && n >= 1 && m >= 1, FPIE_ERR_ARG, "bad arguments");
     *bytes = (double)Batch::job_bytes(n, m);
+  });
+}
+
+int fpie_batch_set_precision(fpie_batch* b, int precision) {
+  return guarded([&] {
+    Batch* h = batch_of(b);
+    FPIE_REQUIRE(precision == FPIE_FP32 || precision == FPIE_MIXED_FP16 ||
+                     precision == FPIE_MIXED_BF16, FPIE_ERR_ARG, "unknown precision");
+    FPIE_REQUIRE(h->live_ids().empty(), FPIE_ERR_STATE,
+                 "set the precision before adding jobs");
+    h->precision = precision;
+  });
+}
+
+int fpie_batch_job_bytes_for(fpie_batch* b, int n, int m, double* bytes) {
+  return guarded([&] {
+    FPIE_REQUIRE(bytes && n >= 1 && m >= 1, FPIE_ERR_ARG, "bad arguments");
+    *bytes = (double)Batch::job_bytes(n, m, batch_of(b)->precision);
   });
 }
 

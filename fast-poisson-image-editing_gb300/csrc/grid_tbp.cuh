@@ -96,7 +96,9 @@ __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __res
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 a = ZS ? z4 : Lanes4<TS, CG>::load(xc + pa);
     const float4 b = ZS ? z4 : Lanes4<TS, CG>::load(xc + pb);
-    const float4 ga = ld4(gc + pa), gb = ld4(gc + pb);
+    // In the persistent batch kernel (CG) "g" may be the residual another CTA
+    // wrote during this launch, so it is read through L2 as well.
+    const float4 ga = Lanes4<float, CG>::load(gc + pa), gb = Lanes4<float, CG>::load(gc + pb);
     P[i][0] = make_float2(a.x, b.x);
     P[i][1] = make_float2(a.y, b.y);
     P[i][2] = make_float2(a.z, b.z);

@@ -54,12 +54,12 @@ class Request:
 class Server:
     def __init__(self, budget_bytes: float = 40e9, epoch_sweeps: int = 256, tol: float = 1e-3,
                  max_sweeps: int = 10000, kernel: str = "auto", batch=None,
-                 job_bytes=None) -> None:
+                 job_bytes=None, precision: str = "fp32") -> None:
         if epoch_sweeps <= 0 or max_sweeps <= 0:
             raise ValueError("epoch_sweeps and max_sweeps must be positive")
         # `batch` / `job_bytes` replace the GPU engine (tests of the host logic).
-        self.batch = batch if batch is not None else BatchSolver(budget_bytes)
-        self.job_bytes = job_bytes or BatchSolver.job_bytes
+        self.batch = batch if batch is not None else BatchSolver(budget_bytes, precision)
+        self.job_bytes = job_bytes or self.batch.job_bytes_for
         if kernel != "auto":
             self.batch.set_kernel(kernel)
         self.budget = budget_bytes
@@ -159,6 +159,7 @@ def run_workload(requests: list[Request], rate: float, seed: int = 0, **server_k
         "sweeps_mean": float(np.mean([r.sweeps for r in srv.finished])),
         "converged": sum(1 for r in srv.finished if r.max_residual <= srv.tol),
         "kernel": srv.batch.kernel,
+        "precision": srv.batch.precision,
     }
 
 
@@ -181,9 +182,11 @@ def main() -> None:
     ap.add_argument("--epoch", type=int, default=256)
     ap.add_argument("--budget-gb", type=float, default=40.0)
     ap.add_argument("--max-box", type=int, default=1024)
+    ap.add_argument("--precision", choices=["fp32", "fp16", "bf16"], default="fp32")
     args = ap.parse_args()
     reqs = make_requests(args.jobs, max_box=args.max_box)
-    stats = run_workload(reqs, args.rate, budget_bytes=args.budget_gb * 1e9, epoch_sweeps=args.epoch)
+    stats = run_workload(reqs, args.rate, budget_bytes=args.budget_gb * 1e9, epoch_sweeps=args.epoch,
+                         precision=args.precision)
     print(json.dumps(stats))
 
 

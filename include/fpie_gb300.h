@@ -219,6 +219,13 @@ int fpie_batch_create(double budget_bytes, fpie_batch** out);
 int fpie_batch_destroy(fpie_batch* b);
 /* Device bytes a job of an n x m grid holds (for admission decisions). */
 int fpie_batch_job_bytes(int n, int m, double* bytes);
+/* Same for this batch's precision (the mixed forms also hold the correction
+ * and residual planes). */
+int fpie_batch_job_bytes_for(fpie_batch* b, int n, int m, double* bytes);
+/* FPIE_FP32 (default) or a mixed form; only before the first job is added.
+ * In the mixed forms every 64 sweeps of a job are 64 correction sweeps
+ * followed by a fold and an FP32 residual, as in fpie_set_precision. */
+int fpie_batch_set_precision(fpie_batch* b, int precision);
 /* Copies the job's inputs (host arrays, layouts as fpie_grid_reset); fails
  * with FPIE_ERR_STATE when the budget has no room.  *job_id receives the
  * slot, reused after fpie_batch_remove. */

@@ -117,3 +117,39 @@ def test_dependency_wait_times_out_without_hanging():
     b.close()
     state, img, err = _alone(mask, t, g, 20)  # the context still works
     assert np.isfinite(state).all()
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+@pytest.mark.parametrize("kernel", ["p16w8k16", "p16w8k8"])
+def test_mixed_batch_equals_mixed_solver(precision, kernel):
+    """Same correction kernel, same cycle boundaries: the batched mixed form
+    reproduces a mixed-precision GridSolver bit for bit."""
+    from fpie_gb300 import backend
+    from fpie_gb300.batch import BatchSolver
+
+    jobs = _jobs(seed=13)
+    b = BatchSolver(4e9, precision=precision)
+    b.set_kernel(kernel)
+    ids = [b.add(mc, t, g, it) for mc, t, g, it in jobs]
+    b.run(200)
+    b.run()
+    for jid, (mc, t, g, it) in zip(ids, jobs):
+        s = backend.GridSolver(8, 8)
+        s.set_precision(precision)
+        s.set_kernel(kernel)
+        s.reset(mc.size, mc, t, g)
+        s.step(min(it, 200))
+        if it > 200:
+            s.step(it - 200)
+        np.testing.assert_array_equal(b.state(jid), s.state())
+
+
+def test_mixed_batch_needs_precision_before_jobs():
+    from fpie_gb300 import _abi
+    from fpie_gb300.batch import BatchSolver
+
+    mc, t, g, it = _jobs()[0]
+    b = BatchSolver(4e9)
+    b.add(mc, t, g, it)
+    with pytest.raises(_abi.FpieError):
+        _abi.call("fpie_batch_set_precision", b._h, 1)

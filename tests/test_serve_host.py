@@ -15,6 +15,8 @@ class FakeBatch:
         self.budget, self.used, self.jobs, self.next_id = budget, 0, {}, 0
         self.run_calls = []
 
+    precision = "fp32"
+
     def memory(self):
         return self.used, self.budget
 
