@@ -446,13 +446,20 @@ def run_batch(args):
         s.sync()
         s.close()
     seq_s = time.perf_counter() - t0
-    # spot parity: three jobs against a GridSolver run of the same kernel
-    same = True
+    # Spot parity: three jobs against a GridSolver run of the same kernel.
+    # FP32 results are bit-identical whatever the kernel; the mixed forms
+    # round the correction where the kernel's depth puts launch boundaries
+    # (the tuner ran other depths for 64 sweeps each), so they are compared
+    # within the mixed forms' tolerance (0.25 FP16, 2.0 BF16 intensity units).
+    same, worst = True, 0.0
+    tol = {"fp32": 0.0, "fp16": 0.25, "bf16": 2.0}[args.precision]
     for k in (0, len(jobs) // 2, len(jobs) - 1):
         mc, t, g, it = jobs[k]
         s = solo(mc, t, g)
         s.step(it)
-        same &= bool(np.array_equal(s.state(), b.state(ids[k])))
+        diff = float(np.abs(s.state() - b.state(ids[k])).max())
+        worst = max(worst, diff)
+        same &= diff <= tol
     line = {"metric": "pixel-updates/s", "value": work / batch_s, "unit": "pixel-updates/s",
             "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": batch_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -464,7 +471,7 @@ def run_batch(args):
                        "batch_kernel": b.kernel, "includes_autotuning": True},
             "sequential_gridsolver": {"value": work / seq_s, "seconds": seq_s},
             "batched_seconds": batch_s, "speedup_vs_sequential": seq_s / batch_s,
-            "gpu_launches": launches, "parity_spot_check": same}
+            "gpu_launches": launches, "parity_spot_check": same, "parity_max_abs_diff": worst}
     print(json.dumps(line), flush=True)
 
 

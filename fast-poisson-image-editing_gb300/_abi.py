@@ -57,6 +57,7 @@ _PROTOS: dict[str, tuple] = {
     "fpie_launch_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
     "fpie_grid_set_kernel": ([_P, ctypes.c_char_p], _I),
     "fpie_grid_kernel": ([_P, ctypes.c_char_p, _I], _I),
+    "fpie_grid_set_spin_limit": ([_P, ctypes.c_longlong], _I),
     "fpie_grid_step_noalloc": ([_I, _I, _P, _P, _P, _I, _P, _P, _P], _I),
     "fpie_residual_norms": ([_P, _P], _I),
     "fpie_grid_solve": ([_P, ctypes.c_double, _I, _I, ctypes.POINTER(_I)], _I),

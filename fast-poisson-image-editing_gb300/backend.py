@@ -177,6 +177,10 @@ class GridSolver(_Solver):
         """Pin the sweep kernel ("auto", "sweep1", or a variant like "r16w8k8")."""
         _abi.call("fpie_grid_set_kernel", self._h, name.encode())
 
+    def set_spin_limit(self, spins: int) -> None:
+        """Polls a resident-kernel neighbour wait may take before the step fails."""
+        _abi.call("fpie_grid_set_spin_limit", self._h, ctypes.c_longlong(int(spins)))
+
     @property
     def kernel(self) -> str:
         buf = ctypes.create_string_buffer(64)

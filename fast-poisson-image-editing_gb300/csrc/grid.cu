@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "grid_kernels.cuh"
 #include "grid_mixed.cuh"
+#include "grid_resident.cuh"
 #include "grid_tb.cuh"
 
 namespace fpie {
@@ -114,6 +115,106 @@ struct GridSolverImpl : Solver {
   static constexpr int kChunk = 64;  // sweeps per captured graph (even)
   cudaGraphExec_t chunk[2] = {nullptr, nullptr};
 
+  // ---- resident kernel state (variant index kResident) -----------------------
+  static constexpr int kResident = -2;
+  int2* r_ctas = nullptr;
+  int* r_nbrs = nullptr;
+  int* r_counters = nullptr;  // [nctas] periods + [1] error flag
+  int r_nctas = 0, r_tiles_x = 0;
+  bool r_ok = false;          // lists built for the current mask
+  int* h_rerr = nullptr;
+  long long r_spin_limit = 1LL << 26;  // x ~64 ns sleeps: a few seconds at most
+
+  void release_resident() {
+    cudaFree(r_ctas);
+    cudaFree(r_nbrs);
+    cudaFree(r_counters);
+    r_ctas = nullptr;
+    r_nbrs = nullptr;
+    r_counters = nullptr;
+    r_nctas = 0;
+    r_ok = false;
+  }
+
+  // Builds the CTA and neighbour lists from the mask (device -> host copy of
+  // the mask plane, once per reset).  Returns false if the problem has more
+  // active (tile, channel) pairs than can be co-resident.
+  bool build_resident() {
+    if (r_ok) return r_nctas > 0;
+    release_resident();
+    const int th = resident_tile_h(), tw = resident_tile_w(), k = resident_depth();
+    const int tx = (G.m + tw - 1) / tw, ty = (G.n + th - 1) / th;
+    std::vector<uint8_t> hm((size_t)G.plane);
+    FPIE_CUDA(cudaMemcpyAsync(hm.data(), mask, (size_t)G.plane, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    std::vector<int> flag(tx * ty, 0);
+    for (int a = 0; a < ty; ++a)
+      for (int b = 0; b < tx; ++b) {
+        bool any = false, all = true;
+        for (int i = a * th - k; i < (a + 1) * th + k; ++i)
+          for (int j = b * tw - k; j < (b + 1) * tw + k; ++j) {
+            const bool in = i >= 0 && i < G.n && j >= 0 && j < G.m;
+            const bool on = in && hm[G.at(i, j)];
+            all = all && on;
+            if (on && i >= a * th && i < (a + 1) * th && j >= b * tw && j < (b + 1) * tw) any = true;
+          }
+        flag[a * tx + b] = any ? (all ? 2 : 1) : 0;
+      }
+    std::vector<int> index(tx * ty * 3, -1);
+    std::vector<int2> ctas;
+    for (int t = 0; t < tx * ty; ++t)
+      if (flag[t])
+        for (int c = 0; c < 3; ++c) {
+          index[t * 3 + c] = (int)ctas.size();
+          ctas.push_back(make_int2(t * 3 + c, flag[t]));
+        }
+    r_ok = true;
+    r_tiles_x = tx;
+    if (ctas.empty() || (int)ctas.size() > resident_max_ctas()) {
+      r_nctas = 0;
+      return false;
+    }
+    std::vector<int> nb(ctas.size() * 8, -1);
+    for (size_t q = 0; q < ctas.size(); ++q) {
+      const int t = ctas[q].x / 3, c = ctas[q].x % 3, a = t / tx, b = t % tx;
+      int n = 0;
+      for (int da = -1; da <= 1; ++da)
+        for (int db = -1; db <= 1; ++db) {
+          if (!da && !db) continue;
+          const int aa = a + da, bb = b + db;
+          if (aa < 0 || aa >= ty || bb < 0 || bb >= tx) continue;
+          const int other = index[(aa * tx + bb) * 3 + c];
+          if (other >= 0) nb[q * 8 + n++] = other;
+        }
+    }
+    r_nctas = (int)ctas.size();
+    FPIE_CUDA(cudaMalloc(&r_ctas, sizeof(int2) * ctas.size()));
+    FPIE_CUDA(cudaMalloc(&r_nbrs, sizeof(int) * nb.size()));
+    FPIE_CUDA(cudaMalloc(&r_counters, sizeof(int) * (ctas.size() + 1)));
+    FPIE_CUDA(cudaMemcpyAsync(r_ctas, ctas.data(), sizeof(int2) * ctas.size(), cudaMemcpyHostToDevice, stream));
+    FPIE_CUDA(cudaMemcpyAsync(r_nbrs, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    return true;
+  }
+
+  // All `iters` sweeps in one cooperative launch.
+  void run_resident(int iters) {
+    FPIE_REQUIRE(build_resident(), FPIE_ERR_ARG,
+                 "the resident kernel needs every active tile of every channel co-resident; "
+                 "this grid has too many tiles for it");
+    if (!h_rerr) FPIE_CUDA(cudaMallocHost(&h_rerr, sizeof(int)));
+    FPIE_CUDA(cudaMemsetAsync(r_counters, 0, sizeof(int) * (r_nctas + 1), stream));
+    launch_resident(G, mask, g, x[cur], x[cur ^ 1], r_ctas, r_nbrs, r_nctas, r_tiles_x, iters,
+                    r_counters, r_counters + r_nctas, r_spin_limit, stream);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(h_rerr, r_counters + r_nctas, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    FPIE_REQUIRE(*h_rerr == 0, FPIE_ERR_TIMEOUT,
+                 "resident kernel: a neighbour wait exceeded its spin limit");
+    const int periods = (iters + resident_depth() - 1) / resident_depth();
+    if (periods & 1) cur ^= 1;
+  }
+
   // ---- mixed-precision refinement state (allocated on first use) -----------
   static constexpr int kRefine = 64;  // inner sweeps per refinement cycle
   void* e[2] = {nullptr, nullptr};    // correction, FP16 or BF16 planes
@@ -142,6 +243,7 @@ struct GridSolverImpl : Solver {
     if (h_err) cudaFreeHost(h_err);
     if (h_norm) cudaFreeHost(h_norm);
     if (h_box) cudaFreeHost(h_box);
+    if (h_rerr) cudaFreeHost(h_rerr);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -187,6 +289,7 @@ struct GridSolverImpl : Solver {
     flags_cap = 0;
     flags_ok = false;
     release_mixed();
+    release_resident();
     if (h_img) cudaFreeHost(h_img);
     x[0] = x[1] = g = nullptr;
     mask = nullptr;
@@ -209,6 +312,7 @@ struct GridSolverImpl : Solver {
       ready = false;
       flags_ok = false;  // the new mask may activate other tiles
       mflags_ok = false;
+      r_ok = false;
       return;
     }
     release();
@@ -330,6 +434,7 @@ struct GridSolverImpl : Solver {
     ready = true;
     flags_ok = false;
     mflags_ok = false;
+    r_ok = false;
     box_out[0] = t_row + x0;
     box_out[1] = t_row + x1;
     box_out[2] = t_col + y0;
@@ -373,7 +478,7 @@ struct GridSolverImpl : Solver {
   int depth() const { return variant < 0 ? 1 : tb_variants()[variant].depth; }
 
   void ensure_flags() {
-    if (variant < 0 || flags_ok) return;
+    if (variant < 0 || flags_ok) return;  // sweep1 / resident need no tile flags
     const TbVariant& v = tb_variants()[variant];
     tiles_x = (G.m + v.tile_w - 1) / v.tile_w;
     tiles = tiles_x * ((G.n + v.tile_h - 1) / v.tile_h);
@@ -457,7 +562,7 @@ struct GridSolverImpl : Solver {
       }
     }
     const int ncand = (int)tb_variants().size() + 1;
-    if (iters < ncand * (kTuneReps + 1) * kChunk + kChunk) return 0;
+    if (iters < (ncand + 1) * (kTuneReps + 1) * kChunk + kChunk) return 0;
     cudaEvent_t e0, e1;
     FPIE_CUDA(cudaEventCreate(&e0));
     FPIE_CUDA(cudaEventCreate(&e1));
@@ -481,6 +586,25 @@ struct GridSolverImpl : Solver {
         }
       }
     }
+    // The resident kernel, when every active tile fits co-resident.
+    if (build_resident() && iters - used >= (kTuneReps + 1) * kChunk) {
+      select_variant(kResident);
+      run_resident(kChunk);
+      used += kChunk;
+      for (int r = 0; r < kTuneReps; ++r) {
+        FPIE_CUDA(cudaEventRecord(e0, stream));
+        run_resident(kChunk);
+        FPIE_CUDA(cudaEventRecord(e1, stream));
+        FPIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        used += kChunk;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = kResident;
+        }
+      }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     select_variant(best);
@@ -498,6 +622,10 @@ struct GridSolverImpl : Solver {
       return;
     }
     if (!tuned && !pinned) iters -= autotune(iters);
+    if (variant == kResident) {
+      if (iters > 0) run_resident(iters);
+      return;
+    }
     while (iters >= kChunk) {
       run_chunk();
       iters -= kChunk;
@@ -720,17 +848,19 @@ struct GridSolverImpl : Solver {
       pinned = true;
       return;
     }
-    int v = -2;
+    int v = -3;
     if (name == "sweep1") v = -1;
+    if (name == "res16w8k4") v = kResident;
     for (size_t k = 0; k < tb_variants().size(); ++k)
       if (name == tb_variants()[k].name) v = (int)k;
-    FPIE_REQUIRE(v != -2, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
+    FPIE_REQUIRE(v != -3, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
     select_variant(v);
     pinned = true;
   }
 
   std::string kernel_name() const {
     if (precision != FPIE_FP32) return std::string(mixed_variants()[mvariant].name);
+    if (variant == kResident) return std::string("res16w8k4");
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }
 
@@ -841,6 +971,13 @@ int fpie_grid_set_kernel(fpie_solver* s, const char* name) {
   return guarded([&] {
     FPIE_REQUIRE(name != nullptr, FPIE_ERR_ARG, "null kernel name");
     grid_of(s)->set_kernel(name);
+  });
+}
+
+int fpie_grid_set_spin_limit(fpie_solver* s, long long spins) {
+  return guarded([&] {
+    FPIE_REQUIRE(spins >= 0, FPIE_ERR_ARG, "spin limit must be >= 0");
+    grid_of(s)->r_spin_limit = spins;
   });
 }
 

@@ -93,13 +93,22 @@ def main() -> None:
             if err <= args.target:
                 hit = done
                 break
+            # Stagnation: no 1% improvement over the last four checkpoints
+            # (plain FP32 Jacobi stalls once a sweep's change rounds away).
+            if len(curve) >= 5 and curve[-1]["max_err"] > 0.99 * curve[-5]["max_err"]:
+                results.setdefault("_stalled", {})[form] = {"sweeps": done, "max_err": err}
+                break
         per_sweep_ms = dev_ms / max(1, done - 4096)
+        stalled = results.get("_stalled", {}).get(form)
         results[form] = {"kernel": s.kernel, "sweeps_to_target": hit,
+                         "stalled_at": stalled,
+                         "best_max_err": min(c["max_err"] for c in curve),
                          "ms_per_sweep": per_sweep_ms,
                          "ms_to_target": per_sweep_ms * hit if hit else None,
                          "px_updates_per_s": unknowns / (per_sweep_ms / 1e3),
                          "curve": curve}
         s.close()
+    results.pop("_stalled", None)
     base = results.get("fp32", {}).get("ms_to_target")
     for form, r in results.items():
         if base and r["ms_to_target"]:
