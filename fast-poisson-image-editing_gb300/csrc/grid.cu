@@ -688,7 +688,7 @@ struct GridSolverImpl : Solver {
   }
 
   // One cycle from x parity `xc`: c inner sweeps on e (from 0), then fold
-  // e into x[xc ^ 1] and compute the new residual and norms.
+  // e into x[xc ^ 1] and compute the new residual.
   void mixed_cycle(cudaStream_t st, int xc, int c) {
     const MixedVariant& v = mixed_variants()[mvariant];
     const MixedVariant::Launch fn =
@@ -701,14 +701,15 @@ struct GridSolverImpl : Solver {
          done == 0 ? 1 : 0, st);
       last = out;
     }
+    // Norms are not needed between cycles (solve() and residual_norms()
+    // compute them from x when asked).
     launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[xc], e[last],
-                  x[xc ^ 1], r, d_part6, st);
-    launch_norms_finalize(d_part6, L.nparts, d_norm, st);
+                  x[xc ^ 1], r, nullptr, st);
   }
 
   int cycle_launches(int c) const {
     const int d = mixed_variants()[mvariant].depth;
-    return (c + d - 1) / d + 2;
+    return (c + d - 1) / d + 1;
   }
 
   void run_cycle_graph() {
@@ -784,8 +785,10 @@ struct GridSolverImpl : Solver {
 
   void run_mixed(int iters) {
     ensure_mixed();
-    refine_norms(stream, r);  // r of the current x starts the first cycle
-    post_launch(this, 2);
+    // r of the current x starts the first cycle (no norms needed here).
+    launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[cur], nullptr, nullptr,
+                  r, nullptr, stream);
+    post_launch(this);
     if (!mtuned && !pinned) iters -= autotune_mixed(iters);
     ensure_mixed();
     while (iters >= kRefine) {

@@ -67,7 +67,8 @@ __device__ __forceinline__ void block_maxsum3(double (&mx)[3], double (&sm)[3]) 
 
 // Thread = 4 adjacent pixels of one row, all channels (the one-sweep
 // kernel's geometry).  e == nullptr: no fold (x is already current);
-// r == nullptr: the residual is only reduced, not stored.
+// r == nullptr: the residual is only reduced, not stored; parts == nullptr:
+// no norm partials (the refinement cycles do not need them).
 template <typename TS>
 __global__ void __launch_bounds__(256)
 grid_refine_kernel(GridGeom G, const uint8_t* __restrict__ mask, const float* __restrict__ g,
@@ -111,6 +112,7 @@ grid_refine_kernel(GridGeom G, const uint8_t* __restrict__ mask, const float* __
       }
     }
   }
+  if (parts == nullptr) return;  // uniform: a kernel argument
   block_maxsum3(mx, sm);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     const long long b = blockIdx.y * (long long)gridDim.x + blockIdx.x;

@@ -7,7 +7,7 @@ namespace fpie {
 
 // x_out = x_in + e (masked pixels; e may be NULL for no fold), r = FP32
 // residual of the folded state (r may be NULL), per-block FP64 max|r| and
-// sum|r| per channel into parts[6*block].  Launch geometry: the one-sweep
+// sum|r| per channel into parts[6*block] (parts may be NULL).  Launch geometry: the one-sweep
 // kernel's (grid_launch(G).sweep_grid / sweep_block).
 void launch_refine(int precision, dim3 grid, dim3 block, const GridGeom& G, const uint8_t* mask,
                    const float* g, const float* xin, const void* e, float* xout, float* r,
