@@ -64,6 +64,10 @@ _PROTOS: dict[str, tuple] = {
     "fpie_grid_reset_images": ([_P, _P, _I, _I, _P, _I, _I, _I, _P, _I, _I, _I, _I, _I, _I, _I,
                                 _I, _P], _I),
     "fpie_grid_get_inputs": ([_P, _P, _P], _I),
+    "fpie_equ_reset_images": ([_P, _P, _I, _I, _P, _I, _I, _I, _P, _I, _I, _I, _I, _I, _I, _I,
+                               _I, _P, ctypes.POINTER(_I)], _I),
+    "fpie_equ_get_index": ([_P, _P, _P], _I),
+    "fpie_equ_get_inputs": ([_P, _P, _P], _I),
     "fpie_batch_create": ([ctypes.c_double, ctypes.POINTER(_P)], _I),
     "fpie_batch_destroy": ([_P], _I),
     "fpie_batch_job_bytes": ([_I, _I, ctypes.POINTER(ctypes.c_double)], _I),

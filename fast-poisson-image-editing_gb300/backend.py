@@ -43,6 +43,28 @@ def _as(a, dtype, shape=None, name="array") -> np.ndarray:
     return out
 
 
+def _image_args(src, mask, tgt, gradient):
+    """Pointers, shapes and codes for the *_reset_images calls (numpy or CUDA tensors)."""
+    mode = {"src": 0, "avg": 1, "max": 2}.get(gradient)
+    if mode is None:
+        raise _abi.FpieArgumentError(f"unknown gradient mode {gradient!r}")
+    on_dev = bool(getattr(src, "is_cuda", False))
+    if on_dev:
+        keep = (src, mask, tgt)
+        ptrs = [_tensor_ptr(a, "uint8", n) for a, n in zip(keep, ("src", "mask", "tgt"))]
+        shapes = [tuple(a.shape) for a in keep]
+    else:
+        keep = tuple(np.ascontiguousarray(a, dtype=np.uint8) for a in (src, mask, tgt))
+        ptrs = [_ptr(a) for a in keep]
+        shapes = [a.shape for a in keep]
+    (sh, sw, sc), msh, (th, tw, tc) = shapes
+    if sc != 3 or tc != 3 or len(msh) not in (2, 3):
+        raise _abi.FpieArgumentError("src/tgt must be HxWx3 and the mask HxW or HxWx3")
+    mch = 1 if len(msh) == 2 else msh[2]
+    args = (ptrs[0], sh, sw, ptrs[1], msh[0], msh[1], mch, ptrs[2], th, tw)
+    return keep, args, mode, on_dev
+
+
 def _tensor_ptr(t, dtype_name: str, name: str) -> int:
     if not t.is_cuda:
         raise _abi.FpieArgumentError(f"{name} must be a CUDA tensor")
@@ -130,6 +152,33 @@ class EquSolver(_Solver):
         _abi.call("fpie_equ_step", self._h, int(iteration), _ptr(x), _ptr(err))
         return x, err
 
+    def reset_images(self, src, mask, tgt, mask_on_src: tuple[int, int],
+                     mask_on_tgt: tuple[int, int], gradient: str = "max"):
+        """Build ids/A/X/B on the GPU from uint8 images (EquProcessor.reset semantics).
+
+        Returns (N, crop box on the target, (rows, cols) target index of unknowns 1..N-1).
+        """
+        keep, args, mode, on_dev = _image_args(src, mask, tgt, gradient)
+        box = (ctypes.c_int * 4)()
+        n_out = ctypes.c_int(0)
+        _abi.call("fpie_equ_reset_images", self._h, *args, int(mask_on_src[0]), int(mask_on_src[1]),
+                  int(mask_on_tgt[0]), int(mask_on_tgt[1]), mode, 1 if on_dev else 0, box,
+                  ctypes.byref(n_out))
+        del keep
+        self.N = n_out.value
+        rows = np.empty(self.N - 1, np.int32)
+        cols = np.empty(self.N - 1, np.int32)
+        if self.N > 1:
+            _abi.call("fpie_equ_get_index", self._h, _ptr(rows), _ptr(cols))
+        return self.N, tuple(box), (rows.astype(np.int64), cols.astype(np.int64))
+
+    def inputs(self) -> tuple[np.ndarray, np.ndarray]:
+        """(A int32[N,4], B float32[N,3]) as the solver holds them."""
+        A = np.empty((self.N, 4), np.int32)
+        B = np.empty((self.N, 3), np.float32)
+        _abi.call("fpie_equ_get_inputs", self._h, _ptr(A), _ptr(B))
+        return A, B
+
     def state(self) -> np.ndarray:
         out = np.empty((self.N, 3), np.float32)
         _abi.call("fpie_get_state", self._h, _ptr(out))
@@ -194,25 +243,11 @@ class GridSolver(_Solver):
         Arrays may be numpy (copied to the device) or torch CUDA uint8 tensors.
         Returns the crop on the target (row0, row1, col0, col1).
         """
-        mode = {"src": 0, "avg": 1, "max": 2}.get(gradient)
-        if mode is None:
-            raise _abi.FpieArgumentError(f"unknown gradient mode {gradient!r}")
-        on_dev = bool(getattr(src, "is_cuda", False))
-        if on_dev:
-            arrs = [_tensor_ptr(a, "uint8", n) for a, n in ((src, "src"), (mask, "mask"), (tgt, "tgt"))]
-            shapes = [tuple(a.shape) for a in (src, mask, tgt)]
-        else:
-            keep = [np.ascontiguousarray(a, dtype=np.uint8) for a in (src, mask, tgt)]
-            arrs = [_ptr(a) for a in keep]
-            shapes = [a.shape for a in keep]
-        (sh, sw, sc), msh, (th, tw, tc) = shapes
-        if sc != 3 or tc != 3 or len(msh) not in (2, 3):
-            raise _abi.FpieArgumentError("src/tgt must be HxWx3 and the mask HxW or HxWx3")
-        mch = 1 if len(msh) == 2 else msh[2]
+        keep, args, mode, on_dev = _image_args(src, mask, tgt, gradient)
         box = (ctypes.c_int * 4)()
-        _abi.call("fpie_grid_reset_images", self._h, arrs[0], sh, sw, arrs[1], msh[0], msh[1], mch,
-                  arrs[2], th, tw, int(mask_on_src[0]), int(mask_on_src[1]), int(mask_on_tgt[0]),
-                  int(mask_on_tgt[1]), mode, 1 if on_dev else 0, box)
+        _abi.call("fpie_grid_reset_images", self._h, *args, int(mask_on_src[0]), int(mask_on_src[1]),
+                  int(mask_on_tgt[0]), int(mask_on_tgt[1]), mode, 1 if on_dev else 0, box)
+        del keep
         self.shape = (box[1] - box[0], box[3] - box[2])
         self.N = self.shape[0] * self.shape[1]
         return tuple(box)

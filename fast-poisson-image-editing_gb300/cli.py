@@ -6,7 +6,7 @@
 Same flags and prints as the reference; ``--check-backend`` lists
 ``ALL_BACKEND`` (the gb300 backends) and exits.  ``-p P`` writes
 ``iterNNNNN.png`` every P sweeps, as the reference does.  ``--device-prep``
-builds the grid inputs on the GPU from the uint8 images.
+builds the solver inputs on the GPU from the uint8 images.
 """
 
 from __future__ import annotations
@@ -49,7 +49,7 @@ def get_args(argv=None) -> argparse.Namespace:
     p.add_argument("--grid-x", type=int, default=8, help="x axis stride for grid solver")
     p.add_argument("--grid-y", type=int, default=8, help="y axis stride for grid solver")
     p.add_argument("--device-prep", action="store_true",
-                   help="grid method: build the solver inputs on the GPU")
+                   help="build the solver inputs on the GPU from the uint8 images")
     args = p.parse_args(argv)
     if args.version:
         print(__version__)
@@ -70,7 +70,8 @@ def main(argv=None) -> None:
     from .process import EquProcessor, GridProcessor
 
     if args.method == "equ":
-        proc = EquProcessor(args.gradient, args.backend, args.cpu, 100, args.block_size)
+        proc = EquProcessor(args.gradient, args.backend, args.cpu, 100, args.block_size,
+                            device_prep=args.device_prep)
     else:
         proc = GridProcessor(args.gradient, args.backend, args.cpu, 100, args.block_size,
                              args.grid_x, args.grid_y, device_prep=args.device_prep)

@@ -8,10 +8,20 @@
 // and neighbour indices validated before any kernel reads through them.
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "common.cuh"
 
 namespace fpie {
+
+void launch_prep_mask(const uint8_t* mask, int mh, int mw, int mch, uint8_t* m01, int* box,
+                      cudaStream_t st);
+int launch_equ_ids(const uint8_t* m01, int mw, int x0, int y0, int n, int m, int* counts,
+                   int* ids, cudaStream_t st);
+void launch_equ_build(const uint8_t* m01, int mw, int x0, int y0, int n, int m, const int* ids,
+                      const uint8_t* src, int sw, int sx, int sy, const uint8_t* tgt, int tw,
+                      int tx, int ty, int mode, long long np, int4* A, float* xa, float* xb,
+                      float* b, int* rows, int* cols, cudaStream_t st);
 
 // X[c][i] planes, `np` floats apart (N rounded up to 32).
 struct EquGeom {
@@ -143,6 +153,8 @@ struct EquSolverImpl : Solver {
 
   ~EquSolverImpl() override {
     release();
+    cudaFree(d_rows);
+    cudaFree(d_cols);
     cudaFree(d_bad);
     if (h_err) cudaFreeHost(h_err);
     if (h_bad) cudaFreeHost(h_bad);
@@ -238,6 +250,106 @@ struct EquSolverImpl : Solver {
     allocate(N);
     FPIE_CUDA(cudaMemcpyAsync(A, dA, (size_t)N * 16, cudaMemcpyDeviceToDevice, stream));
     pack_and_check(dX, dB);
+  }
+
+  int* d_rows = nullptr;  // target coordinates of unknowns 1..N-1 (GPU reset)
+  int* d_cols = nullptr;
+
+  // GPU-side counterpart of EquProcessor.reset (fpie/process.py:293-372):
+  // ids, A, X, B and the unknowns' target coordinates from the uint8 images.
+  // box_out: crop on the target (row0, row1, col0, col1); returns N.
+  int reset_images(const uint8_t* src, int sh, int sw, const uint8_t* msk, int mh, int mw, int mch,
+                   const uint8_t* tgt, int th, int tw, int s_row, int s_col, int t_row, int t_col,
+                   int mode, bool on_device, int* box_out) {
+    FPIE_REQUIRE(src && msk && tgt && box_out, FPIE_ERR_ARG, "null input array");
+    FPIE_REQUIRE(sh > 0 && sw > 0 && mh > 0 && mw > 0 && th > 0 && tw > 0, FPIE_ERR_ARG, "empty image");
+    FPIE_REQUIRE(mch == 1 || mch == 3, FPIE_ERR_ARG, "mask must have 1 or 3 channels");
+    FPIE_REQUIRE(mode >= 0 && mode <= 2, FPIE_ERR_ARG, "gradient mode must be 0 (src), 1 (avg), 2 (max)");
+    const size_t sb = (size_t)sh * sw * 3, mb = (size_t)mh * mw * mch, tb = (size_t)th * tw * 3;
+    const size_t mpx = (size_t)mh * mw;
+    const size_t head = on_device ? 0 : (sb + mb + tb + 15) / 16 * 16;
+    char* stage = nullptr;
+    // staging: images (host path) | box (16 B) | m01 | crop ids (<= mpx ints) | block counts
+    const size_t nb_max = (mpx + 1023) / 1024 + 2;
+    const size_t bytes = head + 16 + (mpx + 15) / 16 * 16 + mpx * 4 + nb_max * 4;
+    FPIE_CUDA(cudaMallocAsync(&stage, bytes, stream));
+    const uint8_t *dsrc = src, *dmsk = msk, *dtgt = tgt;
+    if (!on_device) {
+      FPIE_CUDA(cudaMemcpyAsync(stage, src, sb, cudaMemcpyHostToDevice, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage + sb, msk, mb, cudaMemcpyHostToDevice, stream));
+      FPIE_CUDA(cudaMemcpyAsync(stage + sb + mb, tgt, tb, cudaMemcpyHostToDevice, stream));
+      dsrc = reinterpret_cast<uint8_t*>(stage);
+      dmsk = reinterpret_cast<uint8_t*>(stage + sb);
+      dtgt = reinterpret_cast<uint8_t*>(stage + sb + mb);
+    }
+    int* dbox = reinterpret_cast<int*>(stage + head);
+    uint8_t* m01 = reinterpret_cast<uint8_t*>(stage + head + 16);
+    int* ids = reinterpret_cast<int*>(stage + head + 16 + (mpx + 15) / 16 * 16);
+    int* counts = ids + mpx;
+    int hbox[4] = {INT32_MAX, -1, INT32_MAX, -1};
+    FPIE_CUDA(cudaMemcpyAsync(dbox, hbox, sizeof(hbox), cudaMemcpyHostToDevice, stream));
+    launch_prep_mask(dmsk, mh, mw, mch, m01, dbox, stream);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(hbox, dbox, sizeof(hbox), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    if (hbox[1] < 0) {
+      cudaFreeAsync(stage, stream);
+      throw Error{FPIE_ERR_ARG, "the mask selects no pixel (after clearing its 1-pixel frame)"};
+    }
+    const int x0 = hbox[0] - 1, x1 = hbox[1] + 2, y0 = hbox[2] - 1, y1 = hbox[3] + 2;
+    const bool fits = s_row + x0 >= 0 && s_col + y0 >= 0 && s_row + x1 <= sh && s_col + y1 <= sw &&
+                      t_row + x0 >= 0 && t_col + y0 >= 0 && t_row + x1 <= th && t_col + y1 <= tw;
+    if (!fits) {
+      cudaFreeAsync(stage, stream);
+      throw Error{FPIE_ERR_ARG, "the mask's crop at the given offsets leaves the source or target image"};
+    }
+    const int n = x1 - x0, m = y1 - y0;
+    const int nb = launch_equ_ids(m01, mw, x0, y0, n, m, counts, ids, stream);
+    post_launch(this, 3);
+    int unknowns = 0;
+    FPIE_CUDA(cudaMemcpyAsync(&unknowns, counts + nb, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    const int N = unknowns + 1;
+    allocate(N);
+    cudaFree(d_rows);
+    cudaFree(d_cols);
+    d_rows = d_cols = nullptr;
+    FPIE_CUDA(cudaMalloc(&d_rows, sizeof(int) * std::max(unknowns, 1)));
+    FPIE_CUDA(cudaMalloc(&d_cols, sizeof(int) * std::max(unknowns, 1)));
+    FPIE_CUDA(cudaMemsetAsync(A, 0, sizeof(int4) * N, stream));
+    FPIE_CUDA(cudaMemsetAsync(x[0], 0, (size_t)E.np * 3 * sizeof(float), stream));
+    FPIE_CUDA(cudaMemsetAsync(x[1], 0, (size_t)E.np * 3 * sizeof(float), stream));
+    FPIE_CUDA(cudaMemsetAsync(b, 0, (size_t)E.np * 3 * sizeof(float), stream));
+    launch_equ_build(m01, mw, x0, y0, n, m, ids, dsrc, sw, s_row + x0, s_col + y0, dtgt, tw,
+                     t_row + x0, t_col + y0, mode, E.np, A, x[0], x[1], b, d_rows, d_cols, stream);
+    post_launch(this);
+    FPIE_CUDA(cudaFreeAsync(stage, stream));
+    ready = true;
+    box_out[0] = t_row + x0;
+    box_out[1] = t_row + x1;
+    box_out[2] = t_col + y0;
+    box_out[3] = t_col + y1;
+    if (!on_device) FPIE_CUDA(cudaStreamSynchronize(stream));
+    return N;
+  }
+
+  void get_index(int32_t* rows, int32_t* cols) {
+    FPIE_REQUIRE(rows && cols, FPIE_ERR_ARG, "null output array");
+    FPIE_REQUIRE(ready && d_rows, FPIE_ERR_STATE, "no index: the solver was not reset from images");
+    FPIE_CUDA(cudaMemcpyAsync(rows, d_rows, sizeof(int) * (E.N - 1), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaMemcpyAsync(cols, d_cols, sizeof(int) * (E.N - 1), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  void get_inputs(int32_t* Aout, float* Bout) {
+    FPIE_REQUIRE(Aout && Bout, FPIE_ERR_ARG, "null output array");
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
+    std::vector<float> hb((size_t)E.np * 3);
+    FPIE_CUDA(cudaMemcpyAsync(Aout, A, sizeof(int4) * E.N, cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaMemcpyAsync(hb.data(), b, sizeof(float) * hb.size(), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    for (int i = 0; i < E.N; ++i)
+      for (int c = 0; c < 3; ++c) Bout[(size_t)i * 3 + c] = hb[(size_t)c * E.np + i];
   }
 
   void sweep_once(cudaStream_t st, int from) {
@@ -351,6 +463,27 @@ int fpie_equ_step(fpie_solver* s, int iteration, uint8_t* x_out, float* err_out)
 int fpie_equ_reset_device(fpie_solver* s, int N, const int32_t* A,
                           const float* X, const float* B) {
   return guarded([&] { equ_of(s)->reset_device(N, A, X, B); });
+}
+
+int fpie_equ_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int src_w,
+                          const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
+                          const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
+                          int tgt_row, int tgt_col, int gradient, int on_device, int* box,
+                          int* N_out) {
+  return guarded([&] {
+    const int N = equ_of(s)->reset_images(src, src_h, src_w, mask, mask_h, mask_w, mask_channels,
+                                          tgt, tgt_h, tgt_w, src_row, src_col, tgt_row, tgt_col,
+                                          gradient, on_device != 0, box);
+    if (N_out) *N_out = N;
+  });
+}
+
+int fpie_equ_get_index(fpie_solver* s, int32_t* rows, int32_t* cols) {
+  return guarded([&] { equ_of(s)->get_index(rows, cols); });
+}
+
+int fpie_equ_get_inputs(fpie_solver* s, int32_t* A, float* B) {
+  return guarded([&] { equ_of(s)->get_inputs(A, B); });
 }
 
 int fpie_equ_step_device(fpie_solver* s, int iteration, uint8_t* x, float* err) {

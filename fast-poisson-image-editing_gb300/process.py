@@ -98,8 +98,12 @@ class EquProcessor(BaseProcessor):
     """Equation-form processor: unknowns relabelled, neighbour table A."""
 
     def __init__(self, gradient: str = "max", backend: str = DEFAULT_BACKEND,
-                 n_cpu: int = CPU_COUNT, min_interval: int = 100, block_size: int = 1024):
+                 n_cpu: int = CPU_COUNT, min_interval: int = 100, block_size: int = 1024,
+                 device_prep: bool = False):
+        """device_prep: build ids/A/X/B on the GPU from the uint8 images
+        (fpie_equ_reset_images) instead of with numpy on the host."""
         super().__init__(gradient, 0, backend, _make_core("equ", backend, block_size, 8, 8))
+        self.device_prep = device_prep
 
     def mask2index(self, mask: np.ndarray):
         """ids, N, and the unknowns' (row, col) in id order (fpie/process.py:281-291)."""
@@ -110,6 +114,11 @@ class EquProcessor(BaseProcessor):
         return ids, x.size + 1, x[order], y[order]
 
     def reset(self, src, mask, tgt, mask_on_src, mask_on_tgt) -> int:
+        if self.device_prep:
+            N, _, self.tgt_index = self.core.reset_images(src, mask, tgt, mask_on_src, mask_on_tgt,
+                                                          self.gradient)
+            self.tgt = tgt.copy()
+            return N
         system = prep.equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, self.gradient,
                                  self.core.partition)
         self.tgt = tgt.copy()

@@ -140,6 +140,25 @@ int fpie_grid_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int sr
                            const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
                            int tgt_row, int tgt_col, int gradient, int on_device, int* box);
 
+/* GPU-side counterpart of EquProcessor.reset (fpie/process.py:281-372):
+ * partition (row-major ids of the set pixels, by a prefix scan), A, X, B,
+ * with the same images, offsets and gradient codes as
+ * fpie_grid_reset_images; bit-identical to the host construction.  N_out
+ * receives the unknown count (set pixels + 1); box the crop on the target. */
+int fpie_equ_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int src_w,
+                          const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
+                          const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
+                          int tgt_row, int tgt_col, int gradient, int on_device, int* box,
+                          int* N_out);
+
+/* Target-image coordinates of unknowns 1..N-1 after fpie_equ_reset_images
+ * (the processor's tgt_index, fpie/process.py:370): rows, cols int32[N-1]. */
+int fpie_equ_get_index(fpie_solver* s, int32_t* rows, int32_t* cols);
+
+/* Copies the equation inputs the solver holds: A int32[N][4], B
+ * float32[N][3]. */
+int fpie_equ_get_inputs(fpie_solver* s, int32_t* A, float* B);
+
 /* Copies the grid inputs the solver holds (mask int32[n][m], grad
  * float32[n][m][3]) to host memory. */
 int fpie_grid_get_inputs(fpie_solver* s, int32_t* mask_out, float* grad_out);

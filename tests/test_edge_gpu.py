@@ -1,0 +1,73 @@
+"""Edge cases of the grid and equation solvers against the numpy oracle.
+
+Degenerate and thin grids, no set pixel, every pixel set (borders included,
+so neighbours outside the grid read 0 as in the numpy backend), and sweep
+counts that are not multiples of any kernel's depth -- for every sweep
+kernel.  States bit for bit, images exactly, err rtol 1e-5.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import np_jacobi
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 1), (1, 7), (7, 1), (2, 2), (3, 3), (2, 300), (300, 3), (5, 129), (131, 130)]
+KERNELS = ["sweep1", "r16w8k8", "p16w8k16", "p8w16k8s", "res16w8k4"]
+
+
+def _case(shape, kind, seed):
+    rng = np.random.default_rng(seed)
+    n, m = shape
+    if kind == "none":
+        mask = np.zeros(shape, np.int32)
+    elif kind == "all":
+        mask = np.ones(shape, np.int32)
+    else:
+        mask = (rng.random(shape) > 0.4).astype(np.int32)
+    tgt = rng.uniform(-20, 275, (n, m, 3)).astype(np.float32)  # values outside [0,255] clip
+    grad = rng.uniform(-50, 50, (n, m, 3)).astype(np.float32)
+    return mask, tgt, grad
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("kind", ["none", "all", "random"])
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_grid_edge_cases(shape, kind, kernel):
+    from fpie_gb300 import backend
+
+    mask, tgt, grad = _case(shape, kind, hash((shape, kind)) % 1000)
+    s = backend.GridSolver(8, 8)
+    s.set_kernel(kernel)
+    s.reset(mask.size, mask, tgt, grad)
+    o = np_jacobi.GridJacobi(mask, tgt, grad)
+    for k in (1, 17, 70):
+        img, err = s.step(k)
+        o.sweep(k)
+        np.testing.assert_array_equal(s.state(), o.x)
+        np.testing.assert_array_equal(img, o.image())
+        np.testing.assert_allclose(err, o.err64(), rtol=1e-5, atol=1e-4)
+
+
+@pytest.mark.parametrize("n_unknowns", [1, 2, 33, 1000])
+def test_equ_edge_cases(n_unknowns):
+    """Random neighbour tables, including self-references and row 0 links."""
+    from fpie_gb300 import backend
+
+    rng = np.random.default_rng(n_unknowns)
+    N = n_unknowns
+    A = rng.integers(0, N, (N, 4)).astype(np.int32)
+    X = rng.uniform(-10, 270, (N, 3)).astype(np.float32)
+    B = rng.uniform(-30, 30, (N, 3)).astype(np.float32)
+    s = backend.EquSolver(64)
+    s.reset(N, A, X, B)
+    o = np_jacobi.EquJacobi(A, X, B)
+    for k in (1, 5, 64, 3):
+        x, err = s.step(k)
+        o.sweep(k)
+        np.testing.assert_array_equal(s.state(), o.X)
+        np.testing.assert_array_equal(x, o.image())
+        np.testing.assert_allclose(err, o.err64(), rtol=1e-5, atol=1e-4)

@@ -93,3 +93,49 @@ def test_processor_with_device_prep(golden):
     out, err = proc.step(k)
     x0, x1, y0, y1 = (int(v) for v in d["grid_box"])
     np.testing.assert_array_equal(out[x0:x1, y0:y1], d[f"grid_img_{k}"])
+
+
+def test_equ_inputs_equal_reference(golden):
+    from fpie_gb300 import backend
+
+    name, d = golden
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    s = backend.EquSolver(256)
+    N, box, (rows, cols) = s.reset_images(src, mask, tgt, mos, mot, grad)
+    assert N == int(d["equ_N"])
+    assert box == tuple(int(v) for v in d["grid_box"])
+    A, B = s.inputs()
+    np.testing.assert_array_equal(A, d["equ_A"])
+    np.testing.assert_array_equal(B, d["equ_B"])
+    np.testing.assert_array_equal(s.state(), d["equ_X"])
+    np.testing.assert_array_equal(np.stack([rows, cols]), d["equ_tgt_index"])
+
+
+@pytest.mark.parametrize("gradient", ["src", "avg", "max"])
+def test_equ_square800_equals_host_prep(gradient):
+    from fpie_gb300 import backend, prep, workloads
+
+    pb = workloads.square800()
+    s = backend.EquSolver(256)
+    N, box, idx = s.reset_images(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, gradient)
+    host = prep.equ_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, gradient,
+                           lambda m: np.cumsum((m > 0).reshape(-1)).reshape(m.shape))
+    assert N == host.N == 640001
+    A, B = s.inputs()
+    np.testing.assert_array_equal(A, host.A)
+    np.testing.assert_array_equal(B, host.B)
+    np.testing.assert_array_equal(s.state(), host.X)
+    np.testing.assert_array_equal(np.stack(idx), np.stack(host.tgt_index))
+
+
+def test_equ_processor_with_device_prep(golden):
+    from fpie_gb300.process import EquProcessor
+
+    name, d = golden
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    proc = EquProcessor(gradient=grad, backend="gb300", device_prep=True)
+    proc.reset(src, mask, tgt.copy(), mos, mot)
+    k = int(d["checkpoints"][-1])
+    out, err = proc.step(k)
+    x0, x1, y0, y1 = (int(v) for v in d["grid_box"])
+    np.testing.assert_array_equal(out[x0:x1, y0:y1], d[f"equ_img_{k}"])
