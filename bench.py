@@ -378,6 +378,21 @@ def run_gb300(args):
         "parity": {"timed_output_equals_fresh_solve": same},
     }
 
+    # The FP16 refinement form on the same workload (same step structure).
+    m = backend.GridSolver(8, 8)
+    m.set_stream(stream.cuda_stream)
+    m.set_precision("fp16")
+    m_reset = lambda: m.reset_tensors(dm, dt_, dg)  # noqa: E731
+    m_finish = lambda: m.step_tensors(0, img, err)  # noqa: E731
+    device_steps(args.warmup, m, m_reset, m_finish, False)
+    msteps = max(3, args.steps // 4)
+    mt = device_steps(msteps, m, m_reset, m_finish, True)
+    m_ms = sum(a for a, _ in mt) / msteps
+    line["mixed_fp16"] = {"value": unknowns * sweeps / (m_ms / 1e3), "unit": "pixel-updates/s",
+                          "ms_per_step": m_ms, "steps": msteps, "kernel": m.kernel,
+                          "note": "FP16 correction + FP32 residual every 64 sweeps; equals FP32 "
+                                  "up to the correction's rounding (see the precision study)"}
+
     if not args.no_equ:
         from fpie_gb300 import backend as B
 

@@ -122,10 +122,12 @@ struct GridSolverImpl : Solver {
   int* r_counters = nullptr;  // [nctas] periods + [1] error flag
   int r_nctas = 0, r_tiles_x = 0;
   bool r_ok = false;          // lists built for the current mask
+  bool r_fits = false;        // every active (tile, channel) can be co-resident
   int* h_rerr = nullptr;
   long long r_spin_limit = 1LL << 26;  // x ~64 ns sleeps: a few seconds at most
 
   void release_resident() {
+    r_fits = false;
     cudaFree(r_ctas);
     cudaFree(r_nbrs);
     cudaFree(r_counters);
@@ -138,9 +140,10 @@ struct GridSolverImpl : Solver {
 
   // Builds the CTA and neighbour lists from the mask (device -> host copy of
   // the mask plane, once per reset).  Returns false if the problem has more
-  // active (tile, channel) pairs than can be co-resident.
+  // active (tile, channel) pairs than can be co-resident.  With no active
+  // tile at all it returns true and r_nctas = 0 (sweeps change nothing).
   bool build_resident() {
-    if (r_ok) return r_nctas > 0;
+    if (r_ok) return r_fits;
     release_resident();
     const int th = resident_tile_h(), tw = resident_tile_w(), k = resident_depth();
     const int tx = (G.m + tw - 1) / tw, ty = (G.n + th - 1) / th;
@@ -170,10 +173,9 @@ struct GridSolverImpl : Solver {
         }
     r_ok = true;
     r_tiles_x = tx;
-    if (ctas.empty() || (int)ctas.size() > resident_max_ctas()) {
-      r_nctas = 0;
-      return false;
-    }
+    r_nctas = 0;
+    r_fits = (int)ctas.size() <= resident_max_ctas();
+    if (ctas.empty() || !r_fits) return r_fits;
     std::vector<int> nb(ctas.size() * 8, -1);
     for (size_t q = 0; q < ctas.size(); ++q) {
       const int t = ctas[q].x / 3, c = ctas[q].x % 3, a = t / tx, b = t % tx;
@@ -202,6 +204,7 @@ struct GridSolverImpl : Solver {
     FPIE_REQUIRE(build_resident(), FPIE_ERR_ARG,
                  "the resident kernel needs every active tile of every channel co-resident; "
                  "this grid has too many tiles for it");
+    if (r_nctas == 0) return;  // no masked pixel: sweeps leave the state as it is
     if (!h_rerr) FPIE_CUDA(cudaMallocHost(&h_rerr, sizeof(int)));
     FPIE_CUDA(cudaMemsetAsync(r_counters, 0, sizeof(int) * (r_nctas + 1), stream));
     launch_resident(G, mask, g, x[cur], x[cur ^ 1], r_ctas, r_nbrs, r_nctas, r_tiles_x, iters,
@@ -587,7 +590,7 @@ struct GridSolverImpl : Solver {
       }
     }
     // The resident kernel, when every active tile fits co-resident.
-    if (build_resident() && iters - used >= (kTuneReps + 1) * kChunk) {
+    if (build_resident() && r_nctas > 0 && iters - used >= (kTuneReps + 1) * kChunk) {
       select_variant(kResident);
       run_resident(kChunk);
       used += kChunk;
