@@ -690,49 +690,77 @@ struct GridSolverImpl : Solver {
     launch_norms_finalize(d_part6, L.nparts, d_norm, st);
   }
 
-  // One cycle from x parity `xc`: c inner sweeps on e (from 0), then fold
-  // e into x[xc ^ 1] and compute the new residual.
-  void mixed_cycle(cudaStream_t st, int xc, int c) {
+  // Pending correction: the last cycle's e (in e[e_last]) not yet added to x.
+  bool e_pending = false;
+  int e_last = 0;
+
+  // One refinement cycle of c inner sweeps.  Its first launch folds the
+  // pending correction into x (x[cur] + e -> x[cur ^ 1]), recomputes the
+  // FP32 residual, and starts the new correction from 0 (tbp_fold_body);
+  // the other launches continue the correction.
+  void mixed_cycle(cudaStream_t st, int c) {
     const MixedVariant& v = mixed_variants()[mvariant];
-    const MixedVariant::Launch fn =
-        precision == FPIE_MIXED_BF16 ? v.launch_bf16 : v.launch_fp16;
-    int last = 0;
-    for (int done = 0, k = 0; done < c; done += k) {
+    const bool bf = precision == FPIE_MIXED_BF16;
+    const MixedVariant::Launch fn = bf ? v.launch_bf16 : v.launch_fp16;
+    const MixedVariant::Fold fold = bf ? v.fold_bf16 : v.fold_fp16;
+    const int k0 = std::min(c, v.depth);
+    const int out0 = e_pending ? (e_last ^ 1) : 0;
+    fold(G, mask, g, x[cur], e_pending ? e[e_last] : nullptr, x[cur ^ 1], r, e[out0], mflags,
+         mtiles_x, mtiles, k0, st);
+    if (e_pending) cur ^= 1;
+    int last = out0;
+    for (int done = k0, k = 0; done < c; done += k) {
       k = std::min(c - done, v.depth);
-      const int out = done == 0 ? 0 : last ^ 1;
-      fn(G, mask, r, done == 0 ? nullptr : e[last], e[out], mflags, mtiles_x, mtiles, k,
-         done == 0 ? 1 : 0, st);
-      last = out;
+      fn(G, mask, r, e[last], e[last ^ 1], mflags, mtiles_x, mtiles, k, 0, st);
+      last ^= 1;
     }
-    // Norms are not needed between cycles (solve() and residual_norms()
-    // compute them from x when asked).
-    launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[xc], e[last],
-                  x[xc ^ 1], r, nullptr, st);
+    e_last = last;
+    e_pending = true;
+  }
+
+  // Adds the pending correction to x (end of a step).
+  void mixed_flush(cudaStream_t st) {
+    if (!e_pending) return;
+    launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[cur], e[e_last],
+                  x[cur ^ 1], nullptr, nullptr, st);
+    cur ^= 1;
+    e_pending = false;
   }
 
   int cycle_launches(int c) const {
     const int d = mixed_variants()[mvariant].depth;
-    return (c + d - 1) / d + 1;
+    return (c + d - 1) / d;
   }
 
+  // Full cycles with a pending correction replay captured graphs (one per
+  // x parity; e_last is the same after every full cycle).
   void run_cycle_graph() {
-    if (!cycle[cur]) {
+    if (!e_pending) {  // the first cycle of a step has nothing to fold
+      mixed_cycle(stream, kRefine);
+      post_launch(this, cycle_launches(kRefine));
+      return;
+    }
+    const int key = cur;
+    if (!cycle[key]) {
+      const int save_cur = cur, save_last = e_last;
       cudaStream_t cs = nullptr;
       cudaGraph_t graph = nullptr;
       FPIE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaError_t err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
       if (err == cudaSuccess) {
-        mixed_cycle(cs, cur, kRefine);
+        mixed_cycle(cs, kRefine);
         err = cudaStreamEndCapture(cs, &graph);
       }
-      if (err == cudaSuccess) err = cudaGraphInstantiate(&cycle[cur], graph, 0);
+      if (err == cudaSuccess) err = cudaGraphInstantiate(&cycle[key], graph, 0);
       if (graph) cudaGraphDestroy(graph);
       cudaStreamDestroy(cs);
+      cur = save_cur;  // capturing only recorded the launches
+      e_last = save_last;
       FPIE_CUDA(err);
     }
-    FPIE_CUDA(cudaGraphLaunch(cycle[cur], stream));
+    FPIE_CUDA(cudaGraphLaunch(cycle[key], stream));
     post_launch(this, cycle_launches(kRefine));
-    cur ^= 1;
+    cur ^= 1;  // the cycle's fold moved x
   }
 
   int autotune_mixed(int iters) {
@@ -788,10 +816,7 @@ struct GridSolverImpl : Solver {
 
   void run_mixed(int iters) {
     ensure_mixed();
-    // r of the current x starts the first cycle (no norms needed here).
-    launch_refine(precision, L.sweep_grid, L.sweep_block, G, mask, g, x[cur], nullptr, nullptr,
-                  r, nullptr, stream);
-    post_launch(this);
+    e_pending = false;  // a step starts from a folded x
     if (!mtuned && !pinned) iters -= autotune_mixed(iters);
     ensure_mixed();
     while (iters >= kRefine) {
@@ -799,10 +824,11 @@ struct GridSolverImpl : Solver {
       iters -= kRefine;
     }
     if (iters > 0) {
-      mixed_cycle(stream, cur, iters);
+      mixed_cycle(stream, iters);
       post_launch(this, cycle_launches(iters));
-      cur ^= 1;
     }
+    mixed_flush(stream);
+    post_launch(this);
   }
 
   void residual_norms(double* out) {

@@ -30,6 +30,15 @@ struct MixedVariant {
                           const void* ein, void* eout, const uint8_t* active, int tiles_x,
                           int tiles, int ksweeps, int zero_start, cudaStream_t st);
   Launch launch_fp16, launch_bf16;
+  // First launch of a cycle with the refine step fused in (tbp_fold_body):
+  // xn = x + elast (elast NULL: no fold), r = FP32 residual of xn; writes
+  // xn (tile interiors) to xout, r to rout, and the correction after
+  // ksweeps sweeps from 0 to eout.
+  using Fold = void (*)(const GridGeom& G, const uint8_t* mask, const float* g, const float* xin,
+                        const void* elast, float* xout, float* rout, void* eout,
+                        const uint8_t* active, int tiles_x, int tiles, int ksweeps,
+                        cudaStream_t st);
+  Fold fold_fp16, fold_bf16;
 };
 
 const std::vector<MixedVariant>& mixed_variants();

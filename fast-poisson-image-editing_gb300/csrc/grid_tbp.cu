@@ -53,6 +53,33 @@ grid_tbp_kernel(GridGeom G, const uint8_t* __restrict__ mask,
     tbp_body<R, W, K, false, TS, ZS, false, GS>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
 }
 
+// Fused first launch of a refinement cycle (tbp_fold_body): all channels'
+// tiles, like grid_tbp_kernel.
+template <int R, int W, int K, typename TS, bool HASE>
+__global__ void __launch_bounds__(W * 32)
+grid_tbp_fold_kernel(GridGeom G, const uint8_t* __restrict__ mask, const float* __restrict__ g,
+                     const float* __restrict__ xin, const TS* __restrict__ elast,
+                     float* __restrict__ xout, float* __restrict__ rout, TS* __restrict__ eout,
+                     const uint8_t* __restrict__ active, int tiles_x, int ksweeps) {
+  constexpr int TH = W * R - 2 * K;
+  constexpr int TW = 128 - 2 * K;
+  __shared__ float4 edge[2][2][W][32];
+  const int tile = blockIdx.x;
+  const uint8_t flag = active[tile];
+  if (!flag) return;
+  const int c = blockIdx.y;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+  const long long base = G.at(ty * TH - K + w * R, tx * TW - K + 4 * lane);
+  const long long co = c * G.plane;
+  if (flag == 2)
+    tbp_fold_body<R, W, K, true, TS, HASE>(G, mask, g + co, xin + co, HASE ? elast + co : nullptr,
+                                           xout + co, rout + co, eout + co, base, ksweeps, lane, w, edge);
+  else
+    tbp_fold_body<R, W, K, false, TS, HASE>(G, mask, g + co, xin + co, HASE ? elast + co : nullptr,
+                                            xout + co, rout + co, eout + co, base, ksweeps, lane, w, edge);
+}
+
 namespace {
 
 void no_prepare() {}
@@ -105,6 +132,19 @@ void launch_tbp_lp(const GridGeom& G, const uint8_t* mask, const float* r, const
         ksweeps);
 }
 
+template <int R, int W, int K, typename TS>
+void launch_fold(const GridGeom& G, const uint8_t* mask, const float* g, const float* xin,
+                 const void* elast, float* xout, float* rout, void* eout, const uint8_t* active,
+                 int tiles_x, int tiles, int ksweeps, cudaStream_t st) {
+  if (elast)
+    grid_tbp_fold_kernel<R, W, K, TS, true><<<dim3(tiles, 3), W * 32, 0, st>>>(
+        G, mask, g, xin, static_cast<const TS*>(elast), xout, rout, static_cast<TS*>(eout),
+        active, tiles_x, ksweeps);
+  else
+    grid_tbp_fold_kernel<R, W, K, TS, false><<<dim3(tiles, 3), W * 32, 0, st>>>(
+        G, mask, g, xin, nullptr, xout, rout, static_cast<TS*>(eout), active, tiles_x, ksweeps);
+}
+
 template <int R, int W, int K>
 MixedVariant make_mixed(const char* name) {
   MixedVariant v;
@@ -114,6 +154,8 @@ MixedVariant make_mixed(const char* name) {
   v.tile_w = 128 - 2 * K;
   v.launch_fp16 = &launch_tbp_lp<R, W, K, __half>;
   v.launch_bf16 = &launch_tbp_lp<R, W, K, __nv_bfloat16>;
+  v.fold_fp16 = &launch_fold<R, W, K, __half>;
+  v.fold_bf16 = &launch_fold<R, W, K, __nv_bfloat16>;
   return v;
 }
 

@@ -72,52 +72,13 @@ __device__ __forceinline__ float2 pick2(uint32_t ma, uint32_t mb, uint32_t bit,
   return make_float2((ma & bit) ? upd.x : old.x, (mb & bit) ? upd.y : old.y);
 }
 
-// TS: storage type of the swept state (float for the plain solver; __half
-// or __nv_bfloat16 for the correction of the mixed form).  zero_start: the
-// state starts at 0 instead of being loaded (first inner launch of a
-// refinement cycle).
-// GS: the grad pairs live in shared memory (sg: this warp's H x 32 x 4
-// float2, i.e. W*R*32*16 bytes per CTA, dynamic) instead of registers,
-// freeing 4R registers per thread for taller regions.
-template <int R, int W, int K, bool FULL, typename TS, bool ZS, bool CG = false, bool GS = false>
-__device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __restrict__ mask,
-                                         const float* __restrict__ gc,
-                                         const TS* __restrict__ xc, TS* __restrict__ oc,
-                                         long long base, int ksweeps,
-                                         int lane, int w, float4 (&edge)[2][2][W][32],
-                                         float2* __restrict__ sg = nullptr) {
+// ksweeps packed sweeps of the strip held in P (pairs of rows i, i+R/2),
+// grad pairs in Gp (or shared memory sg when GS), mask words in mk.
+template <int R, int W, bool FULL, bool GS>
+__device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (&Gp)[GS ? 1 : R / 2][4],
+                                           const uint32_t (&mk)[R], int ksweeps, int lane, int w,
+                                           float4 (&edge)[2][2][W][32], const float2* __restrict__ sg) {
   constexpr int H = R / 2;
-  float2 P[H][4], Gp[GS ? 1 : H][4];
-  uint32_t mk[R];
-#pragma unroll
-  for (int i = 0; i < H; ++i) {
-    const long long pa = base + (long long)i * G.pitch;
-    const long long pb = base + (long long)(i + H) * G.pitch;
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 a = ZS ? z4 : Lanes4<TS, CG>::load(xc + pa);
-    const float4 b = ZS ? z4 : Lanes4<TS, CG>::load(xc + pb);
-    // In the persistent batch kernel (CG) "g" may be the residual another CTA
-    // wrote during this launch, so it is read through L2 as well.
-    const float4 ga = Lanes4<float, CG>::load(gc + pa), gb = Lanes4<float, CG>::load(gc + pb);
-    P[i][0] = make_float2(a.x, b.x);
-    P[i][1] = make_float2(a.y, b.y);
-    P[i][2] = make_float2(a.z, b.z);
-    P[i][3] = make_float2(a.w, b.w);
-    if (GS) {
-      float2* q = sg + ((size_t)i * 32 + lane) * 4;
-      *reinterpret_cast<float4*>(q) = make_float4(ga.x, gb.x, ga.y, gb.y);
-      *reinterpret_cast<float4*>(q + 2) = make_float4(ga.z, gb.z, ga.w, gb.w);
-    } else {
-      Gp[GS ? 0 : i][0] = make_float2(ga.x, gb.x);
-      Gp[GS ? 0 : i][1] = make_float2(ga.y, gb.y);
-      Gp[GS ? 0 : i][2] = make_float2(ga.z, gb.z);
-      Gp[GS ? 0 : i][3] = make_float2(ga.w, gb.w);
-    }
-    if (!FULL) {
-      mk[i] = __ldg(reinterpret_cast<const unsigned int*>(mask + pa));
-      mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
-    }
-  }
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
   const float2 q = make_float2(0.25f, 0.25f);
   for (int s = 0; s < ksweeps; ++s) {
@@ -179,6 +140,55 @@ __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __res
       }
     }
   }
+}
+
+// TS: storage type of the swept state (float for the plain solver; __half
+// or __nv_bfloat16 for the correction of the mixed form).  zero_start: the
+// state starts at 0 instead of being loaded (first inner launch of a
+// refinement cycle).
+// GS: the grad pairs live in shared memory (sg: this warp's H x 32 x 4
+// float2, i.e. W*R*32*16 bytes per CTA, dynamic) instead of registers,
+// freeing 4R registers per thread for taller regions.
+template <int R, int W, int K, bool FULL, typename TS, bool ZS, bool CG = false, bool GS = false>
+__device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __restrict__ mask,
+                                         const float* __restrict__ gc,
+                                         const TS* __restrict__ xc, TS* __restrict__ oc,
+                                         long long base, int ksweeps,
+                                         int lane, int w, float4 (&edge)[2][2][W][32],
+                                         float2* __restrict__ sg = nullptr) {
+  constexpr int H = R / 2;
+  float2 P[H][4], Gp[GS ? 1 : H][4];
+  uint32_t mk[R];
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const long long pa = base + (long long)i * G.pitch;
+    const long long pb = base + (long long)(i + H) * G.pitch;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 a = ZS ? z4 : Lanes4<TS, CG>::load(xc + pa);
+    const float4 b = ZS ? z4 : Lanes4<TS, CG>::load(xc + pb);
+    // In the persistent batch kernel (CG) "g" may be the residual another CTA
+    // wrote during this launch, so it is read through L2 as well.
+    const float4 ga = Lanes4<float, CG>::load(gc + pa), gb = Lanes4<float, CG>::load(gc + pb);
+    P[i][0] = make_float2(a.x, b.x);
+    P[i][1] = make_float2(a.y, b.y);
+    P[i][2] = make_float2(a.z, b.z);
+    P[i][3] = make_float2(a.w, b.w);
+    if (GS) {
+      float2* q = sg + ((size_t)i * 32 + lane) * 4;
+      *reinterpret_cast<float4*>(q) = make_float4(ga.x, gb.x, ga.y, gb.y);
+      *reinterpret_cast<float4*>(q + 2) = make_float4(ga.z, gb.z, ga.w, gb.w);
+    } else {
+      Gp[GS ? 0 : i][0] = make_float2(ga.x, gb.x);
+      Gp[GS ? 0 : i][1] = make_float2(ga.y, gb.y);
+      Gp[GS ? 0 : i][2] = make_float2(ga.z, gb.z);
+      Gp[GS ? 0 : i][3] = make_float2(ga.w, gb.w);
+    }
+    if (!FULL) {
+      mk[i] = __ldg(reinterpret_cast<const unsigned int*>(mask + pa));
+      mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
+    }
+  }
+  tbp_sweeps<R, W, FULL, GS>(P, Gp, mk, ksweeps, lane, w, edge, sg);
   if (lane >= K / 4 && lane < 32 - K / 4) {
 #pragma unroll
     for (int i = 0; i < H; ++i) {
@@ -188,6 +198,119 @@ __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __res
                           make_float4(P[i][0].x, P[i][1].x, P[i][2].x, P[i][3].x));
       if (rb >= K && rb < W * R - K)
         Lanes4<TS>::store(oc + base + (long long)(i + H) * G.pitch,
+                          make_float4(P[i][0].y, P[i][1].y, P[i][2].y, P[i][3].y));
+    }
+  }
+}
+
+// First inner launch of a refinement cycle with the refine step fused in:
+// loads x (FP32) and, when HASE, the previous cycle's correction e, forms
+// xn = x + e and the FP32 residual r = -(4xn - g - up - down - left - right)
+// (the refine kernel's formula, so values are identical) on the whole
+// region in registers -- the outermost ring, whose neighbours lie outside,
+// gets a wrong r, which like every region-border error cannot reach the
+// tile in K sweeps -- writes xn (if HASE) and r for the tile interior, then
+// runs ksweeps correction sweeps from e = 0 and writes e for the tile.
+template <int R, int W, int K, bool FULL, typename TS, bool HASE>
+__device__ __forceinline__ void tbp_fold_body(const GridGeom& G, const uint8_t* __restrict__ mask,
+                                              const float* __restrict__ gc,
+                                              const float* __restrict__ xin,
+                                              const TS* __restrict__ elast,
+                                              float* __restrict__ xout, float* __restrict__ rout,
+                                              TS* __restrict__ eout, long long base, int ksweeps,
+                                              int lane, int w, float4 (&edge)[2][2][W][32]) {
+  constexpr int H = R / 2;
+  float2 P[H][4], Gp[H][4];
+  uint32_t mk[R];
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const long long pa = base + (long long)i * G.pitch;
+    const long long pb = base + (long long)(i + H) * G.pitch;
+    float4 a = ld4(xin + pa), b = ld4(xin + pb);
+    if (HASE) {
+      const float4 ea = Lanes4<TS>::load(elast + pa), eb = Lanes4<TS>::load(elast + pb);
+      a = make_float4(__fadd_rn(a.x, ea.x), __fadd_rn(a.y, ea.y), __fadd_rn(a.z, ea.z), __fadd_rn(a.w, ea.w));
+      b = make_float4(__fadd_rn(b.x, eb.x), __fadd_rn(b.y, eb.y), __fadd_rn(b.z, eb.z), __fadd_rn(b.w, eb.w));
+    }
+    const float4 ga = ld4(gc + pa), gb = ld4(gc + pb);
+    P[i][0] = make_float2(a.x, b.x);
+    P[i][1] = make_float2(a.y, b.y);
+    P[i][2] = make_float2(a.z, b.z);
+    P[i][3] = make_float2(a.w, b.w);
+    Gp[i][0] = make_float2(ga.x, gb.x);
+    Gp[i][1] = make_float2(ga.y, gb.y);
+    Gp[i][2] = make_float2(ga.z, gb.z);
+    Gp[i][3] = make_float2(ga.w, gb.w);
+    mk[i] = __ldg(reinterpret_cast<const unsigned int*>(mask + pa));
+    mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
+  }
+  // Residual of xn (edge slot 1; the sweeps below start with slot 0).
+  {
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    edge[1][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+    edge[1][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+    __syncthreads();
+    const float4 above = w > 0 ? edge[1][1][w - 1][lane] : zero;
+    const float4 below = w < W - 1 ? edge[1][0][w + 1][lane] : zero;
+    float2 up[4] = {make_float2(above.x, P[H - 1][0].x), make_float2(above.y, P[H - 1][1].x),
+                    make_float2(above.z, P[H - 1][2].x), make_float2(above.w, P[H - 1][3].x)};
+    const float2 dlast[4] = {make_float2(P[0][0].y, below.x), make_float2(P[0][1].y, below.y),
+                             make_float2(P[0][2].y, below.z), make_float2(P[0][3].y, below.w)};
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      const float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
+      float2 dn[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dn[j] = i < H - 1 ? P[i + 1][j] : dlast[j];
+      const float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cur[3].x, 1),
+                                    __shfl_up_sync(0xffffffffu, cur[3].y, 1));
+      const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
+                                    __shfl_down_sync(0xffffffffu, cur[0].y, 1));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float2 l = j > 0 ? cur[j - 1] : lf;
+        const float2 r = j < 3 ? cur[j + 1] : rt;
+        const uint32_t bit = 0xffu << (8 * j);
+        const float ra = (mk[i] & bit) ? -grid_res(cur[j].x, Gp[i][j].x, up[j].x, dn[j].x, l.x, r.x) : 0.0f;
+        const float rb = (mk[i + H] & bit) ? -grid_res(cur[j].y, Gp[i][j].y, up[j].y, dn[j].y, l.y, r.y) : 0.0f;
+        up[j] = cur[j];
+        Gp[i][j] = make_float2(ra, rb);  // the residual becomes the sweeps' right-hand side
+      }
+    }
+  }
+  if (lane >= K / 4 && lane < 32 - K / 4) {
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      const int ra = w * R + i, rb = ra + H;
+      const long long pa = base + (long long)i * G.pitch, pb = base + (long long)(i + H) * G.pitch;
+      if (ra >= K && ra < W * R - K) {
+        if (HASE && mk[i])
+          *reinterpret_cast<float4*>(xout + pa) = make_float4(P[i][0].x, P[i][1].x, P[i][2].x, P[i][3].x);
+        *reinterpret_cast<float4*>(rout + pa) =
+            make_float4(Gp[i][0].x, Gp[i][1].x, Gp[i][2].x, Gp[i][3].x);
+      }
+      if (rb >= K && rb < W * R - K) {
+        if (HASE && mk[i + H])
+          *reinterpret_cast<float4*>(xout + pb) = make_float4(P[i][0].y, P[i][1].y, P[i][2].y, P[i][3].y);
+        *reinterpret_cast<float4*>(rout + pb) =
+            make_float4(Gp[i][0].y, Gp[i][1].y, Gp[i][2].y, Gp[i][3].y);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < H; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) P[i][j] = make_float2(0.f, 0.f);
+  tbp_sweeps<R, W, FULL, false>(P, Gp, mk, ksweeps, lane, w, edge, nullptr);
+  if (lane >= K / 4 && lane < 32 - K / 4) {
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      const int ra = w * R + i, rb = ra + H;
+      if (ra >= K && ra < W * R - K)
+        Lanes4<TS>::store(eout + base + (long long)i * G.pitch,
+                          make_float4(P[i][0].x, P[i][1].x, P[i][2].x, P[i][3].x));
+      if (rb >= K && rb < W * R - K)
+        Lanes4<TS>::store(eout + base + (long long)(i + H) * G.pitch,
                           make_float4(P[i][0].y, P[i][1].y, P[i][2].y, P[i][3].y));
     }
   }
