@@ -45,43 +45,46 @@ struct BJobDev {
   int parity;       // buffer holding the state at level 0
 };
 
-// Level schedule of the mixed forms for a launch of S sweeps with depth K:
-// level 0 computes the residual of x; then every cycle of up to 64 sweeps
-// has ceil(len/K) inner levels on the correction (the first starting from
-// 0) and one fold level (x += e into the other x buffer, new residual).
+// Level schedule of the mixed forms for a launch of S sweeps with depth K
+// (P = 64 / K launches per full cycle): every cycle of up to 64 sweeps is
+// ceil(len / K) inner levels, the first of which folds the previous
+// cycle's correction into x and recomputes the residual (tbp_fold_body);
+// one flush level at the end folds the last correction.  The x buffer
+// flips once per fold: C = ceil(S / 64) times per launch.
 struct MixedLevel {
-  int type;    // 0 = residual, 1 = inner, 2 = fold
-  int k;       // inner: sweeps
-  int pos;     // inner: index within the cycle (0 = zero start)
-  int cycle;   // fold / inner: cycle index (x parity offset)
-  int ninner;  // inner levels of this cycle
+  int type;   // 0 = fold + first inner, 1 = inner, 2 = flush
+  int k;      // sweeps of an inner level
+  int pos;    // index within the cycle
+  int cycle;
+  int nlast;  // levels of the last cycle
 };
 
 __host__ __device__ inline int mixed_levels(int S, int K) {
-  const int P = 64 / K, C = S / 64, rem = S % 64;
-  return 1 + C * (P + 1) + (rem ? (rem + K - 1) / K + 1 : 0);
+  const int P = 64 / K, C = (S + 63) / 64;
+  const int nlast = (S - 64 * (C - 1) + K - 1) / K;
+  return (C - 1) * P + nlast + 1;
 }
 
 __host__ __device__ inline MixedLevel mixed_level(int z, int S, int K) {
-  MixedLevel L{0, 0, 0, 0, 0};
-  if (z == 0) return L;
-  const int P = 64 / K, C = S / 64, rem = S % 64;
-  int zz = z - 1, cyc = zz / (P + 1), pos = zz % (P + 1), len = 64, ninner = P;
-  if (cyc >= C) {  // the last, partial cycle
-    cyc = C;
-    pos = zz - C * (P + 1);
-    len = rem;
-    ninner = (rem + K - 1) / K;
-  }
-  L.cycle = cyc;
-  L.ninner = ninner;
-  if (pos < ninner) {
-    L.type = 1;
-    L.pos = pos;
-    L.k = len - pos * K < K ? len - pos * K : K;
-  } else {
+  const int P = 64 / K, C = (S + 63) / 64, nfull = C - 1;
+  const int nlast = (S - 64 * nfull + K - 1) / K;
+  MixedLevel L{0, 0, 0, 0, nlast};
+  if (z == nfull * P + nlast) {
     L.type = 2;
+    L.cycle = C;
+    return L;
   }
+  int len = 64;
+  if (z < nfull * P) {
+    L.cycle = z / P;
+    L.pos = z % P;
+  } else {
+    L.cycle = nfull;
+    L.pos = z - nfull * P;
+    len = S - 64 * nfull;
+  }
+  L.k = len - L.pos * K < K ? len - L.pos * K : K;
+  L.type = L.pos == 0 ? 0 : 1;
   return L;
 }
 
@@ -127,7 +130,7 @@ __device__ void refine_tile(const GridGeom& G, const uint8_t* __restrict__ mask,
       const bool on = (mk >> (8 * k)) & 0xffu;
       rr[k] = on ? -grid_res(xv[k + 1], g4[k], u4[k], d4[k], xv[k], xv[k + 2]) : 0.0f;
     }
-    *reinterpret_cast<float4*>(r + p) = make_float4(rr[0], rr[1], rr[2], rr[3]);
+    if (r) *reinterpret_cast<float4*>(r + p) = make_float4(rr[0], rr[1], rr[2], rr[3]);
   }
 }
 
@@ -212,27 +215,38 @@ batch_persistent_kernel(BQueue Q) {
         tbp_body<R, W, K, false, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
     } else {
       const MixedLevel L = mixed_level(z, J.sweeps, K);
-      const int xp = (J.parity + L.cycle) & 1;
       TS* e0 = static_cast<TS*>(J.e[0]);
       TS* e1 = static_cast<TS*>(J.e[1]);
-      if (L.type == 1) {
+      if (L.type == 0) {
+        // x parity before this cycle's fold: one flip per earlier fold.
+        const int xp = (J.parity + (L.cycle > 0 ? L.cycle - 1 : 0)) & 1;
+        if (L.cycle > 0) {  // full previous cycles end in e[1]
+          if (tf.y == 2)
+            tbp_fold_body<R, W, K, true, TS, true, true>(J.G, J.mask, gc, J.x[xp] + co, e1 + co,
+                J.x[xp ^ 1] + co, J.r + co, e0 + co, base, L.k, lane, w, edge);
+          else
+            tbp_fold_body<R, W, K, false, TS, true, true>(J.G, J.mask, gc, J.x[xp] + co, e1 + co,
+                J.x[xp ^ 1] + co, J.r + co, e0 + co, base, L.k, lane, w, edge);
+        } else {
+          if (tf.y == 2)
+            tbp_fold_body<R, W, K, true, TS, false, true>(J.G, J.mask, gc, J.x[xp] + co, nullptr,
+                nullptr, J.r + co, e0 + co, base, L.k, lane, w, edge);
+          else
+            tbp_fold_body<R, W, K, false, TS, false, true>(J.G, J.mask, gc, J.x[xp] + co, nullptr,
+                nullptr, J.r + co, e0 + co, base, L.k, lane, w, edge);
+        }
+      } else if (L.type == 1) {
         const TS* ein = ((L.pos - 1) & 1) ? e1 : e0;
         TS* eout = (L.pos & 1) ? e1 : e0;
         const float* rc = J.r + co;
-        if (L.pos == 0) {
-          if (tf.y == 2)
-            tbp_body<R, W, K, true, TS, true, true>(J.G, J.mask, rc, nullptr, eout + co, base, L.k, lane, w, edge);
-          else
-            tbp_body<R, W, K, false, TS, true, true>(J.G, J.mask, rc, nullptr, eout + co, base, L.k, lane, w, edge);
-        } else {
-          if (tf.y == 2)
-            tbp_body<R, W, K, true, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
-          else
-            tbp_body<R, W, K, false, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
-        }
+        if (tf.y == 2)
+          tbp_body<R, W, K, true, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
+        else
+          tbp_body<R, W, K, false, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
       } else {
-        const TS* elast = L.type == 2 ? (((L.ninner - 1) & 1) ? e1 : e0) + co : nullptr;
-        refine_tile<TS>(J.G, J.mask, gc, J.x[xp] + co, elast, J.x[xp ^ 1] + co, J.r + co,
+        const int xp = (J.parity + L.cycle - 1) & 1;
+        const TS* elast = (((L.nlast - 1) & 1) ? e1 : e0) + co;
+        refine_tile<TS>(J.G, J.mask, gc, J.x[xp] + co, elast, J.x[xp ^ 1] + co, nullptr,
                         ty * TH, tx * TW, TH, TW);
       }
     }
@@ -420,8 +434,8 @@ struct Batch {
       FPIE_CUDA(cudaMemsetAsync(j.g, 0, 3 * pb, stream));
       FPIE_CUDA(cudaMemsetAsync(j.mask, 0, (size_t)j.G.plane, stream));
       const size_t px = (size_t)n * m;
-      char* stage = nullptr;
-      FPIE_CUDA(cudaMallocAsync(&stage, px * 28, stream));
+      AsyncScratch scratch(px * 28, stream);
+      char* stage = scratch.bytes();
       FPIE_CUDA(cudaMemcpyAsync(stage, hm, px * 4, cudaMemcpyHostToDevice, stream));
       FPIE_CUDA(cudaMemcpyAsync(stage + px * 4, ht, px * 12, cudaMemcpyHostToDevice, stream));
       FPIE_CUDA(cudaMemcpyAsync(stage + px * 16, hg, px * 12, cudaMemcpyHostToDevice, stream));
@@ -431,7 +445,6 @@ struct Batch {
           reinterpret_cast<float*>(stage + px * 16), j.mask, j.x[0], j.x[1], j.g);
       FPIE_CUDA(cudaGetLastError());
       ++launches;
-      FPIE_CUDA(cudaFreeAsync(stage, stream));
       FPIE_CUDA(cudaStreamSynchronize(stream));  // the caller may reuse its arrays
     } catch (...) {
       free_job(j);
@@ -531,8 +544,8 @@ struct Batch {
       const size_t bytes = al(b_jobs) + al(b_order) + al(b_ct) + al(b_lo) + al(b_act) +
                            al(b_tiles) + al(b_done) + 256;
       std::vector<char> host(bytes, 0);
-      char* dev = nullptr;
-      FPIE_CUDA(cudaMallocAsync(&dev, bytes, stream));
+      AsyncScratch tables(bytes, stream);
+      char* dev = tables.bytes();
       size_t off = 0;
       auto put = [&](const void* src, size_t n) {
         if (n) std::memcpy(host.data() + off, src, n);
@@ -571,7 +584,6 @@ struct Batch {
       if (time_it) FPIE_CUDA(cudaEventRecord(e1, stream));
       int herr = 0;
       FPIE_CUDA(cudaMemcpyAsync(&herr, q.error, sizeof(int), cudaMemcpyDeviceToHost, stream));
-      FPIE_CUDA(cudaFreeAsync(dev, stream));
       FPIE_CUDA(cudaStreamSynchronize(stream));
       if (time_it) {
         FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));

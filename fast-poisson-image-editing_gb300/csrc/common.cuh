@@ -51,6 +51,22 @@ int guarded(F&& body) {
   }
 }
 
+// Stream-ordered device scratch that is released on every exit path,
+// exceptions included (cudaFreeAsync on the stream it was allocated on).
+struct AsyncScratch {
+  void* ptr = nullptr;
+  cudaStream_t stream = nullptr;
+  AsyncScratch(size_t bytes, cudaStream_t st) : stream(st) {
+    FPIE_CUDA(cudaMallocAsync(&ptr, bytes, st));
+  }
+  ~AsyncScratch() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+  }
+  AsyncScratch(const AsyncScratch&) = delete;
+  AsyncScratch& operator=(const AsyncScratch&) = delete;
+  char* bytes() const { return static_cast<char*>(ptr); }
+};
+
 // ---- grid geometry ----------------------------------------------------------
 // The grid state lives in HBM as three planar float32 channel planes with a
 // zero halo of kPad rows above and kPad columns left of the crop, and

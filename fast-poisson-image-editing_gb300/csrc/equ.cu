@@ -235,13 +235,12 @@ struct EquSolverImpl : Solver {
   void reset_host(int N, const int32_t* hA, const float* hX, const float* hB) {
     FPIE_REQUIRE(hA && hX && hB, FPIE_ERR_ARG, "null input array");
     allocate(N);
-    float* stage = nullptr;
-    FPIE_CUDA(cudaMallocAsync(&stage, (size_t)N * 24, stream));
+    AsyncScratch scratch((size_t)N * 24, stream);
+    float* stage = reinterpret_cast<float*>(scratch.bytes());
     FPIE_CUDA(cudaMemcpyAsync(A, hA, (size_t)N * 16, cudaMemcpyHostToDevice, stream));
     FPIE_CUDA(cudaMemcpyAsync(stage, hX, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
     FPIE_CUDA(cudaMemcpyAsync(stage + (size_t)N * 3, hB, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
     pack_and_check(stage, stage + (size_t)N * 3);
-    FPIE_CUDA(cudaFreeAsync(stage, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 
@@ -268,11 +267,11 @@ struct EquSolverImpl : Solver {
     const size_t sb = (size_t)sh * sw * 3, mb = (size_t)mh * mw * mch, tb = (size_t)th * tw * 3;
     const size_t mpx = (size_t)mh * mw;
     const size_t head = on_device ? 0 : (sb + mb + tb + 15) / 16 * 16;
-    char* stage = nullptr;
     // staging: images (host path) | box (16 B) | m01 | crop ids (<= mpx ints) | block counts
     const size_t nb_max = (mpx + 1023) / 1024 + 2;
     const size_t bytes = head + 16 + (mpx + 15) / 16 * 16 + mpx * 4 + nb_max * 4;
-    FPIE_CUDA(cudaMallocAsync(&stage, bytes, stream));
+    AsyncScratch scratch(bytes, stream);
+    char* stage = scratch.bytes();
     const uint8_t *dsrc = src, *dmsk = msk, *dtgt = tgt;
     if (!on_device) {
       FPIE_CUDA(cudaMemcpyAsync(stage, src, sb, cudaMemcpyHostToDevice, stream));
@@ -292,17 +291,13 @@ struct EquSolverImpl : Solver {
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(hbox, dbox, sizeof(hbox), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
-    if (hbox[1] < 0) {
-      cudaFreeAsync(stage, stream);
+    if (hbox[1] < 0)
       throw Error{FPIE_ERR_ARG, "the mask selects no pixel (after clearing its 1-pixel frame)"};
-    }
     const int x0 = hbox[0] - 1, x1 = hbox[1] + 2, y0 = hbox[2] - 1, y1 = hbox[3] + 2;
     const bool fits = s_row + x0 >= 0 && s_col + y0 >= 0 && s_row + x1 <= sh && s_col + y1 <= sw &&
                       t_row + x0 >= 0 && t_col + y0 >= 0 && t_row + x1 <= th && t_col + y1 <= tw;
-    if (!fits) {
-      cudaFreeAsync(stage, stream);
+    if (!fits)
       throw Error{FPIE_ERR_ARG, "the mask's crop at the given offsets leaves the source or target image"};
-    }
     const int n = x1 - x0, m = y1 - y0;
     const int nb = launch_equ_ids(m01, mw, x0, y0, n, m, counts, ids, stream);
     post_launch(this, 3);
@@ -323,7 +318,6 @@ struct EquSolverImpl : Solver {
     launch_equ_build(m01, mw, x0, y0, n, m, ids, dsrc, sw, s_row + x0, s_col + y0, dtgt, tw,
                      t_row + x0, t_col + y0, mode, E.np, A, x[0], x[1], b, d_rows, d_cols, stream);
     post_launch(this);
-    FPIE_CUDA(cudaFreeAsync(stage, stream));
     ready = true;
     box_out[0] = t_row + x0;
     box_out[1] = t_row + x1;
@@ -413,12 +407,11 @@ struct EquSolverImpl : Solver {
   void get_state(float* out) {
     FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
-    float* tmp = nullptr;
-    FPIE_CUDA(cudaMallocAsync(&tmp, (size_t)E.N * 12, stream));
+    AsyncScratch scratch((size_t)E.N * 12, stream);
+    float* tmp = reinterpret_cast<float*>(scratch.bytes());
     equ_unpack_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, x[cur], tmp);
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(out, tmp, (size_t)E.N * 12, cudaMemcpyDeviceToHost, stream));
-    FPIE_CUDA(cudaFreeAsync(tmp, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 };

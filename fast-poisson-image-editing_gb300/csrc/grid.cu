@@ -353,9 +353,9 @@ struct GridSolverImpl : Solver {
     allocate(n, m);
     N_user = N;
     const size_t px = (size_t)n * m;
-    char* stage = nullptr;
     const size_t bytes = px * 4 + 2 * px * 12;
-    FPIE_CUDA(cudaMallocAsync(&stage, bytes, stream));
+    AsyncScratch scratch(bytes, stream);
+    char* stage = scratch.bytes();
     int32_t* sm = reinterpret_cast<int32_t*>(stage);
     float* st = reinterpret_cast<float*>(stage + px * 4);
     float* sg = reinterpret_cast<float*>(stage + px * 16);
@@ -363,7 +363,6 @@ struct GridSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(st, ht, px * 12, cudaMemcpyHostToDevice, stream));
     FPIE_CUDA(cudaMemcpyAsync(sg, hg, px * 12, cudaMemcpyHostToDevice, stream));
     pack(sm, st, sg);
-    FPIE_CUDA(cudaFreeAsync(stage, stream));
     // The caller may reuse its arrays as soon as reset returns.
     FPIE_CUDA(cudaStreamSynchronize(stream));
   }
@@ -390,9 +389,9 @@ struct GridSolverImpl : Solver {
                  "gradient mode must be 0 (src), 1 (avg), 2 (max)");
     const size_t sb = (size_t)sh * sw * 3, mb = (size_t)mh * mw * mch, tb = (size_t)th * tw * 3;
     const size_t mpx = (size_t)mh * mw;
-    char* stage = nullptr;
     const size_t head = on_device ? 0 : (sb + mb + tb + 15) / 16 * 16;
-    FPIE_CUDA(cudaMallocAsync(&stage, head + 16 + mpx, stream));
+    AsyncScratch scratch(head + 16 + mpx, stream);
+    char* stage = scratch.bytes();
     const uint8_t *dsrc = src, *dmsk = msk, *dtgt = tgt;
     if (!on_device) {
       FPIE_CUDA(cudaMemcpyAsync(stage, src, sb, cudaMemcpyHostToDevice, stream));
@@ -415,25 +414,20 @@ struct GridSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(h_box, dbox, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
     const int b0 = h_box[0], b1 = h_box[1], b2 = h_box[2], b3 = h_box[3];
-    if (b1 < 0) {
-      cudaFreeAsync(stage, stream);
+    if (b1 < 0)
       throw Error{FPIE_ERR_ARG, "the mask selects no pixel (after clearing its 1-pixel frame)"};
-    }
     const int x0 = b0 - 1, x1 = b1 + 2, y0 = b2 - 1, y1 = b3 + 2;
     const bool fits = s_row + x0 >= 0 && s_col + y0 >= 0 && s_row + x1 <= sh && s_col + y1 <= sw &&
                       t_row + x0 >= 0 && t_col + y0 >= 0 && t_row + x1 <= th && t_col + y1 <= tw;
-    if (!fits) {
-      cudaFreeAsync(stage, stream);
+    if (!fits)
       throw Error{FPIE_ERR_ARG,
                   "the mask's crop at the given offsets leaves the source or target image"};
-    }
     allocate(x1 - x0, y1 - y0);
     N_user = G.n * G.m;
     PrepArgs a{G, m01, mw, x0, y0, dsrc, sw, s_row + x0, s_col + y0, dtgt, tw, t_row + x0,
                t_col + y0, mode};
     launch_prep_grid(a, mask, x[0], x[1], g, stream);
     post_launch(this);
-    FPIE_CUDA(cudaFreeAsync(stage, stream));
     ready = true;
     flags_ok = false;
     mflags_ok = false;
@@ -449,14 +443,13 @@ struct GridSolverImpl : Solver {
     FPIE_REQUIRE(mask_out && grad_out, FPIE_ERR_ARG, "null output array");
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
     const long long total = (long long)G.n * G.m;
-    char* tmp = nullptr;
-    FPIE_CUDA(cudaMallocAsync(&tmp, total * 16, stream));
+    AsyncScratch scratch(total * 16, stream);
+    char* tmp = scratch.bytes();
     grid_inputs_unpack_kernel<<<conv_blocks(total), 256, 0, stream>>>(
         G, mask, g, reinterpret_cast<int32_t*>(tmp), reinterpret_cast<float*>(tmp + total * 4));
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(mask_out, tmp, total * 4, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaMemcpyAsync(grad_out, tmp + total * 4, total * 12, cudaMemcpyDeviceToHost, stream));
-    FPIE_CUDA(cudaFreeAsync(tmp, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 
@@ -933,12 +926,11 @@ struct GridSolverImpl : Solver {
     FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
     const long long total = (long long)G.n * G.m;
-    float* tmp = nullptr;
-    FPIE_CUDA(cudaMallocAsync(&tmp, total * 12, stream));
+    AsyncScratch scratch(total * 12, stream);
+    float* tmp = reinterpret_cast<float*>(scratch.bytes());
     grid_unpack_kernel<<<conv_blocks(total), 256, 0, stream>>>(G, x[cur], tmp);
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(out, tmp, total * 12, cudaMemcpyDeviceToHost, stream));
-    FPIE_CUDA(cudaFreeAsync(tmp, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 };

@@ -211,7 +211,7 @@ __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __res
 // gets a wrong r, which like every region-border error cannot reach the
 // tile in K sweeps -- writes xn (if HASE) and r for the tile interior, then
 // runs ksweeps correction sweeps from e = 0 and writes e for the tile.
-template <int R, int W, int K, bool FULL, typename TS, bool HASE>
+template <int R, int W, int K, bool FULL, typename TS, bool HASE, bool CG = false>
 __device__ __forceinline__ void tbp_fold_body(const GridGeom& G, const uint8_t* __restrict__ mask,
                                               const float* __restrict__ gc,
                                               const float* __restrict__ xin,
@@ -226,9 +226,9 @@ __device__ __forceinline__ void tbp_fold_body(const GridGeom& G, const uint8_t* 
   for (int i = 0; i < H; ++i) {
     const long long pa = base + (long long)i * G.pitch;
     const long long pb = base + (long long)(i + H) * G.pitch;
-    float4 a = ld4(xin + pa), b = ld4(xin + pb);
+    float4 a = Lanes4<float, CG>::load(xin + pa), b = Lanes4<float, CG>::load(xin + pb);
     if (HASE) {
-      const float4 ea = Lanes4<TS>::load(elast + pa), eb = Lanes4<TS>::load(elast + pb);
+      const float4 ea = Lanes4<TS, CG>::load(elast + pa), eb = Lanes4<TS, CG>::load(elast + pb);
       a = make_float4(__fadd_rn(a.x, ea.x), __fadd_rn(a.y, ea.y), __fadd_rn(a.z, ea.z), __fadd_rn(a.w, ea.w));
       b = make_float4(__fadd_rn(b.x, eb.x), __fadd_rn(b.y, eb.y), __fadd_rn(b.z, eb.z), __fadd_rn(b.w, eb.w));
     }
