@@ -227,7 +227,8 @@ class GridSolver(_Solver):
         _abi.call("fpie_grid_set_kernel", self._h, name.encode())
 
     def set_spin_limit(self, spins: int) -> None:
-        """Polls a resident-kernel neighbour wait may take before the step fails."""
+        """Polls a resident-kernel neighbour wait, or a TMA-kernel copy wait,
+        may take before the step fails with FpieTimeoutError."""
         _abi.call("fpie_grid_set_spin_limit", self._h, ctypes.c_longlong(int(spins)))
 
     @property

@@ -178,6 +178,9 @@ struct Solver {
   long long launches = 0;
   int precision = FPIE_FP32;
   virtual ~Solver() {}
+  // Raises the error a kernel recorded in device memory (e.g. a bounded wait
+  // that timed out); called after the stream has been synchronised.
+  virtual void check_async() {}
   void activate() const { FPIE_CUDA(cudaSetDevice(device)); }
 };
 

@@ -19,6 +19,7 @@
 #include "grid_kernels.cuh"
 #include "grid_mixed.cuh"
 #include "grid_resident.cuh"
+#include "grid_tma.cuh"
 #include "grid_tb.cuh"
 
 namespace fpie {
@@ -125,6 +126,27 @@ struct GridSolverImpl : Solver {
   bool r_fits = false;        // every active (tile, channel) can be co-resident
   int* h_rerr = nullptr;
   long long r_spin_limit = 1LL << 26;  // x ~64 ns sleeps: a few seconds at most
+
+  // ---- persistent TMA-prefetch kernel (variant index kTma) -------------------
+  static constexpr int kTma = -3;
+  int* d_tma_err = nullptr;  // set by a copy wait that timed out
+  int* h_tma_err = nullptr;  // pinned
+  int tma_grid = 0;          // persistent CTAs for the current tiling
+
+  // Reads and clears the TMA kernel's time-out flag; call after the stream
+  // has been synchronised.
+  void check_tma() {
+    if (!d_tma_err) return;
+    FPIE_CUDA(cudaMemcpyAsync(h_tma_err, d_tma_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    if (*h_tma_err) {
+      *h_tma_err = 0;
+      FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
+      FPIE_CUDA(cudaStreamSynchronize(stream));
+      throw Error{FPIE_ERR_TIMEOUT, "TMA sweep kernel: a wait for a region copy timed out"};
+    }
+  }
+  void check_async() override { check_tma(); }
 
   void release_resident() {
     r_fits = false;
@@ -293,6 +315,10 @@ struct GridSolverImpl : Solver {
     flags_ok = false;
     release_mixed();
     release_resident();
+    cudaFree(d_tma_err);
+    if (h_tma_err) cudaFreeHost(h_tma_err);
+    d_tma_err = nullptr;
+    h_tma_err = nullptr;
     if (h_img) cudaFreeHost(h_img);
     x[0] = x[1] = g = nullptr;
     mask = nullptr;
@@ -471,21 +497,38 @@ struct GridSolverImpl : Solver {
     return 0;
   }
 
-  int depth() const { return variant < 0 ? 1 : tb_variants()[variant].depth; }
+  int depth() const {
+    if (variant == kTma) return tma_depth();
+    return variant < 0 ? 1 : tb_variants()[variant].depth;
+  }
 
   void ensure_flags() {
-    if (variant < 0 || flags_ok) return;  // sweep1 / resident need no tile flags
-    const TbVariant& v = tb_variants()[variant];
-    tiles_x = (G.m + v.tile_w - 1) / v.tile_w;
-    tiles = tiles_x * ((G.n + v.tile_h - 1) / v.tile_h);
+    if (flags_ok || (variant < 0 && variant != kTma)) return;  // sweep1 / resident: no flags
+    const bool tma = variant == kTma;
+    const int th = tma ? tma_tile_h() : tb_variants()[variant].tile_h;
+    const int tw = tma ? tma_tile_w() : tb_variants()[variant].tile_w;
+    const int kd = tma ? tma_depth() : tb_variants()[variant].depth;
+    tiles_x = (G.m + tw - 1) / tw;
+    tiles = tiles_x * ((G.n + th - 1) / th);
     if (tiles > flags_cap) {
       cudaFree(flags);
       flags = nullptr;
       FPIE_CUDA(cudaMalloc(&flags, tiles));
       flags_cap = tiles;
     }
-    v.prepare();
-    launch_tile_flags(G, mask, v.tile_h, v.tile_w, v.depth, tiles_x, tiles, flags, stream);
+    if (tma) {
+      prepare_tma();
+      tma_grid = tma_ctas(tiles * 3);
+      if (!d_tma_err) {
+        FPIE_CUDA(cudaMalloc(&d_tma_err, sizeof(int)));
+        FPIE_CUDA(cudaMallocHost(&h_tma_err, sizeof(int)));
+        *h_tma_err = 0;
+        FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
+      }
+    } else {
+      tb_variants()[variant].prepare();
+    }
+    launch_tile_flags(G, mask, th, tw, kd, tiles_x, tiles, flags, stream);
     post_launch(this);
     flags_ok = true;
   }
@@ -500,7 +543,10 @@ struct GridSolverImpl : Solver {
 
   // k sweeps (k <= depth()) from buffer `from`; flips nothing (caller does).
   void launch_block(cudaStream_t st, int from, int k) {
-    if (variant < 0) {
+    if (variant == kTma) {
+      launch_tma(G, mask, g, x[from], x[from ^ 1], flags, tiles_x, tiles, k, d_tma_err, r_spin_limit,
+                 tma_grid, st);
+    } else if (variant < 0) {
       launch_grid_sweep(L, G, mask, g, x[from], x[from ^ 1], st);
     } else {
       const TbVariant& v = tb_variants()[variant];
@@ -557,14 +603,18 @@ struct GridSolverImpl : Solver {
         return 0;
       }
     }
-    const int ncand = (int)tb_variants().size() + 1;
+    // Candidates: sweep1, every temporally blocked variant, the TMA kernel.
+    std::vector<int> cands{-1};
+    for (int v = 0; v < (int)tb_variants().size(); ++v) cands.push_back(v);
+    cands.push_back(kTma);
+    const int ncand = (int)cands.size();
     if (iters < (ncand + 1) * (kTuneReps + 1) * kChunk + kChunk) return 0;
     cudaEvent_t e0, e1;
     FPIE_CUDA(cudaEventCreate(&e0));
     FPIE_CUDA(cudaEventCreate(&e1));
     int best = default_variant(), used = 0;
     float best_ms = 1e30f;
-    for (int v = -1; v < ncand - 1; ++v) {
+    for (int v : cands) {
       select_variant(v);
       run_chunk();  // warm: flags, graph capture, first replay
       used += kChunk;
@@ -873,12 +923,13 @@ struct GridSolverImpl : Solver {
       pinned = true;
       return;
     }
-    int v = -3;
+    int v = -100;  // unknown
     if (name == "sweep1") v = -1;
     if (name == "res16w8k4") v = kResident;
+    if (name == "p16w8k16t") v = kTma;
     for (size_t k = 0; k < tb_variants().size(); ++k)
       if (name == tb_variants()[k].name) v = (int)k;
-    FPIE_REQUIRE(v != -3, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
+    FPIE_REQUIRE(v != -100, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
     select_variant(v);
     pinned = true;
   }
@@ -886,6 +937,7 @@ struct GridSolverImpl : Solver {
   std::string kernel_name() const {
     if (precision != FPIE_FP32) return std::string(mixed_variants()[mvariant].name);
     if (variant == kResident) return std::string("res16w8k4");
+    if (variant == kTma) return std::string("p16w8k16t");
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }
 
@@ -918,6 +970,7 @@ struct GridSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(h_img, d_img, bytes, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaMemcpyAsync(h_err, d_err, 3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
+    check_tma();
     std::memcpy(img_out, h_img, bytes);
     std::memcpy(err_out, h_err, 3 * sizeof(float));
   }
@@ -932,6 +985,7 @@ struct GridSolverImpl : Solver {
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(out, tmp, total * 12, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
+    check_tma();
   }
 };
 
@@ -1001,7 +1055,9 @@ int fpie_grid_set_kernel(fpie_solver* s, const char* name) {
 int fpie_grid_set_spin_limit(fpie_solver* s, long long spins) {
   return guarded([&] {
     FPIE_REQUIRE(spins >= 0, FPIE_ERR_ARG, "spin limit must be >= 0");
-    grid_of(s)->r_spin_limit = spins;
+    GridSolverImpl* h = grid_of(s);
+    if (spins != h->r_spin_limit) h->drop_graphs();  // captured TMA launches hold the limit
+    h->r_spin_limit = spins;
   });
 }
 

@@ -86,6 +86,7 @@ int fpie_sync(fpie_solver* s) {
   return guarded([&] {
     Solver* h = check_handle(s, 0);
     FPIE_CUDA(cudaStreamSynchronize(h->stream));
+    h->check_async();
   });
 }
 

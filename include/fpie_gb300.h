@@ -195,7 +195,9 @@ int fpie_grid_set_kernel(fpie_solver* s, const char* name);
 
 /* The resident kernel ("res16w8k4", grids whose active tiles all fit
  * co-resident) waits for neighbour tiles between its 4-sweep periods; each
- * wait gives up after `spins` polls (~64 ns apart) and the step returns
+ * wait gives up after `spins` polls (~64 ns apart).  The TMA kernel
+ * ("p16w8k16t") waits for its region copies; each wait gives up after
+ * `spins` polls.  Either way the step (or fpie_sync) returns
  * FPIE_ERR_TIMEOUT, leaving the state undefined.  Default 2^26. */
 int fpie_grid_set_spin_limit(fpie_solver* s, long long spins);
 

@@ -127,7 +127,7 @@ def test_tensor_handoff(backend):
 
 KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16", "r16w10k8s",
            "r16w12k8s", "r12w16k16s", "p16w8k8", "p16w8k16", "p8w16k16", "p8w12k8",
-           "p16w8k4", "p12w12k8s", "p8w16k8s", "res16w8k4"]
+           "p16w8k4", "p12w12k8s", "p8w16k8s", "res16w8k4", "p16w8k16t"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -214,3 +214,56 @@ def test_resident_wait_times_out_without_hanging(backend):
     u.reset(int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
     u.step(50)
     np.testing.assert_array_equal(u.state(), d["grid_state_50"])
+
+
+def _many_items_case():
+    """1500x1700 grid: 288 tiles x 3 channels = 864 (tile, channel) items, so
+    every persistent CTA of the TMA kernel sweeps several, prefetching each
+    next region during the current one's sweeps.  Empty top rows (inactive
+    tiles, skipped), a solid right half (fully masked tiles) and a holed left
+    half (tiles with unmasked pixels)."""
+    rng = np.random.default_rng(5)
+    n, m = 1500, 1700
+    mask = np.zeros((n, m), np.int32)
+    mask[200:1450, 60:1650] = 1
+    holes = rng.random((n, m)) < 0.03
+    holes[:, 850:] = False
+    mask[holes] = 0
+    tgt = rng.uniform(0, 255, (n, m, 3)).astype(np.float32)
+    grad = rng.uniform(-30, 30, (n, m, 3)).astype(np.float32)
+    grad[mask == 0] = 0
+    return mask, tgt, grad
+
+
+def test_tma_kernel_many_items_per_cta(backend):
+    mask, tgt, grad = _many_items_case()
+    s = backend.GridSolver(8, 8)
+    s.set_kernel("p16w8k16t")
+    s.reset(mask.size, mask, tgt, grad)
+    o = cjacobi.CGrid(mask, tgt, grad)
+    for k in (1, 15, 130):  # a 1-sweep launch, a partial block, graph chunks
+        img, err = s.step(k)
+        o.sweep(k)
+        np.testing.assert_array_equal(s.state(), o.x)
+    np.testing.assert_array_equal(img, o.image())
+
+
+def test_tma_wait_times_out_without_hanging(backend):
+    """A spin limit of 0 makes a region-copy wait give up: the step returns a
+    timeout error (after the CTA's copies in flight have landed) instead of
+    hanging, and the solver and GPU stay usable."""
+    from fpie_gb300 import _abi
+
+    mc, t, g, _ = _square800_grid()
+    s = backend.GridSolver(8, 8)
+    s.set_kernel("p16w8k16t")
+    s.set_spin_limit(0)
+    s.reset(mc.size, mc, t, g)
+    with pytest.raises(_abi.FpieTimeoutError):
+        s.step(64)
+    s.set_spin_limit(1 << 26)
+    s.reset(mc.size, mc, t, g)
+    s.step(100)
+    o = cjacobi.CGrid(mc, t, g)
+    o.sweep(100)
+    np.testing.assert_array_equal(s.state(), o.x)
