@@ -131,6 +131,8 @@ struct GridSolverImpl : Solver {
   static constexpr int kTma = -3;
   int* d_tma_err = nullptr;  // set by a copy wait that timed out
   int* h_tma_err = nullptr;  // pinned
+  int* tma_list = nullptr;   // active-tile list (count + indices)
+  int tma_list_cap = 0;
   int tma_grid = 0;          // persistent CTAs for the current tiling
 
   // Reads and clears the TMA kernel's time-out flag; call after the stream
@@ -316,9 +318,12 @@ struct GridSolverImpl : Solver {
     release_mixed();
     release_resident();
     cudaFree(d_tma_err);
+    cudaFree(tma_list);
     if (h_tma_err) cudaFreeHost(h_tma_err);
     d_tma_err = nullptr;
     h_tma_err = nullptr;
+    tma_list = nullptr;
+    tma_list_cap = 0;
     if (h_img) cudaFreeHost(h_img);
     x[0] = x[1] = g = nullptr;
     mask = nullptr;
@@ -525,11 +530,21 @@ struct GridSolverImpl : Solver {
         *h_tma_err = 0;
         FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
       }
+      if (tiles + 1 > tma_list_cap) {
+        cudaFree(tma_list);
+        tma_list = nullptr;
+        FPIE_CUDA(cudaMalloc(&tma_list, (size_t)(tiles + 1) * sizeof(int)));
+        tma_list_cap = tiles + 1;
+      }
     } else {
       tb_variants()[variant].prepare();
     }
     launch_tile_flags(G, mask, th, tw, kd, tiles_x, tiles, flags, stream);
     post_launch(this);
+    if (tma) {
+      launch_tma_list(flags, tiles, tma_list, stream);
+      post_launch(this);
+    }
     flags_ok = true;
   }
 
@@ -544,8 +559,8 @@ struct GridSolverImpl : Solver {
   // k sweeps (k <= depth()) from buffer `from`; flips nothing (caller does).
   void launch_block(cudaStream_t st, int from, int k) {
     if (variant == kTma) {
-      launch_tma(G, mask, g, x[from], x[from ^ 1], flags, tiles_x, tiles, k, d_tma_err, r_spin_limit,
-                 tma_grid, st);
+      launch_tma(G, mask, g, x[from], x[from ^ 1], flags, tma_list, tiles_x, tiles, k, d_tma_err,
+                 r_spin_limit, tma_grid, st);
     } else if (variant < 0) {
       launch_grid_sweep(L, G, mask, g, x[from], x[from ^ 1], st);
     } else {

@@ -72,74 +72,129 @@ __device__ __forceinline__ float2 pick2(uint32_t ma, uint32_t mb, uint32_t bit,
   return make_float2((ma & bit) ? upd.x : old.x, (mb & bit) ? upd.y : old.y);
 }
 
-// ksweeps packed sweeps of the strip held in P (pairs of rows i, i+R/2),
-// grad pairs in Gp (or shared memory sg when GS), mask words in mk.
-template <int R, int W, bool FULL, bool GS>
-__device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (&Gp)[GS ? 1 : R / 2][4],
-                                           const uint32_t (&mk)[R], int ksweeps, int lane, int w,
-                                           float4 (&edge)[2][2][W][32], const float2* __restrict__ sg) {
+// Grad pair row i (registers, or this warp's shared-memory copy when GS).
+template <int R, bool GS>
+__device__ __forceinline__ void tbp_grad(const float2 (&Gp)[GS ? 1 : R / 2][4],
+                                         const float2* __restrict__ sg, int i, int lane,
+                                         float2 (&gv)[4]) {
+  if (GS) {
+    const float4* q = reinterpret_cast<const float4*>(sg + ((size_t)i * 32 + lane) * 4);
+    const float4 a = q[0], b = q[1];
+    gv[0] = make_float2(a.x, a.y);
+    gv[1] = make_float2(a.z, a.w);
+    gv[2] = make_float2(b.x, b.y);
+    gv[3] = make_float2(b.z, b.w);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) gv[j] = Gp[GS ? 0 : i][j];
+  }
+}
+
+// New values of pair row i from its old value `cur` and the old pairs above
+// and below: ((((g + up) + down) + left) + right) * 0.25 per lane, the numpy
+// order, with unmasked pixels keeping `cur`.
+template <int R, bool FULL>
+__device__ __forceinline__ void tbp_update(const float2 (&cur)[4], const float2 (&up)[4],
+                                           const float2 (&dn)[4], const float2 (&gv)[4],
+                                           const uint32_t (&mk)[R], int i, float2 (&o)[4]) {
+  constexpr int H = R / 2;
+  const float2 q = make_float2(0.25f, 0.25f);
+  const float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cur[3].x, 1),
+                                __shfl_up_sync(0xffffffffu, cur[3].y, 1));
+  const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
+                                __shfl_down_sync(0xffffffffu, cur[0].y, 1));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float2 l = j > 0 ? cur[j - 1] : lf;
+    const float2 r = j < 3 ? cur[j + 1] : rt;
+    float2 t = __fadd2_rn(gv[j], up[j]);
+    t = __fadd2_rn(t, dn[j]);
+    t = __fadd2_rn(t, l);
+    t = __fadd2_rn(t, r);
+    o[j] = __fmul2_rn(t, q);
+  }
+  if (!FULL) {
+    o[0] = pick2(mk[i], mk[i + H], 0x000000ffu, o[0], cur[0]);
+    o[1] = pick2(mk[i], mk[i + H], 0x0000ff00u, o[1], cur[1]);
+    o[2] = pick2(mk[i], mk[i + H], 0x00ff0000u, o[2], cur[2]);
+    o[3] = pick2(mk[i], mk[i + H], 0xff000000u, o[3], cur[3]);
+  }
+}
+
+// One sweep of the strip held in P (pairs of rows i, i+R/2), using edge
+// buffer `par`.  FWD visits pair rows 0..H-1 keeping a copy of each old row
+// as the next row's "up"; !FWD visits H-1..0 keeping the old row as the
+// next row's "down".  In registers a forward sweep leaves each new row where
+// the old row above it was, and a backward sweep moves it back, so a
+// forward + backward pair needs no register copies at the loop's back edge.
+// Either order computes the same values (Jacobi: every update reads old
+// values only).
+template <int R, int W, bool FULL, bool GS, bool FWD>
+__device__ __forceinline__ void tbp_sweep(float2 (&P)[R / 2][4], const float2 (&Gp)[GS ? 1 : R / 2][4],
+                                          const uint32_t (&mk)[R], int par, int lane, int w,
+                                          float4 (&edge)[2][2][W][32], const float2* __restrict__ sg) {
   constexpr int H = R / 2;
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float2 q = make_float2(0.25f, 0.25f);
-  for (int s = 0; s < ksweeps; ++s) {
-    const int par = s & 1;
-    edge[par][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
-    edge[par][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
-    __syncthreads();
-    const float4 above = w > 0 ? edge[par][1][w - 1][lane] : zero;
-    const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
-    // Pair 0's up: (row -1 from the warp above, row H-1 own).
-    float2 up[4] = {make_float2(above.x, P[H - 1][0].x), make_float2(above.y, P[H - 1][1].x),
-                    make_float2(above.z, P[H - 1][2].x), make_float2(above.w, P[H - 1][3].x)};
-    // Pair H-1's down: (row H own, row R from the warp below).
-    const float2 dlast[4] = {make_float2(P[0][0].y, below.x), make_float2(P[0][1].y, below.y),
-                             make_float2(P[0][2].y, below.z), make_float2(P[0][3].y, below.w)};
+  edge[par][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+  edge[par][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+  __syncthreads();
+  const float4 above = w > 0 ? edge[par][1][w - 1][lane] : zero;
+  const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
+  // Pair 0's up: (row -1 from the warp above, row H-1 own).
+  const float2 ufirst[4] = {make_float2(above.x, P[H - 1][0].x), make_float2(above.y, P[H - 1][1].x),
+                            make_float2(above.z, P[H - 1][2].x), make_float2(above.w, P[H - 1][3].x)};
+  // Pair H-1's down: (row H own, row R from the warp below).
+  const float2 dlast[4] = {make_float2(P[0][0].y, below.x), make_float2(P[0][1].y, below.y),
+                           make_float2(P[0][2].y, below.z), make_float2(P[0][3].y, below.w)};
+  if (FWD) {
+    float2 up[4] = {ufirst[0], ufirst[1], ufirst[2], ufirst[3]};
 #pragma unroll
     for (int i = 0; i < H; ++i) {
-      float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
-      float2 dn[4];
+      const float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
+      float2 dn[4], gv[4], o[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) dn[j] = i < H - 1 ? P[i + 1][j] : dlast[j];
-      const float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cur[3].x, 1),
-                                    __shfl_up_sync(0xffffffffu, cur[3].y, 1));
-      const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
-                                    __shfl_down_sync(0xffffffffu, cur[0].y, 1));
-      float2 gv[4];
-      if (GS) {
-        const float4* q = reinterpret_cast<const float4*>(sg + ((size_t)i * 32 + lane) * 4);
-        const float4 a = q[0], b = q[1];
-        gv[0] = make_float2(a.x, a.y);
-        gv[1] = make_float2(a.z, a.w);
-        gv[2] = make_float2(b.x, b.y);
-        gv[3] = make_float2(b.z, b.w);
-      } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) gv[j] = Gp[GS ? 0 : i][j];
-      }
-      float2 o[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float2 l = j > 0 ? cur[j - 1] : lf;
-        const float2 r = j < 3 ? cur[j + 1] : rt;
-        float2 t = __fadd2_rn(gv[j], up[j]);
-        t = __fadd2_rn(t, dn[j]);
-        t = __fadd2_rn(t, l);
-        t = __fadd2_rn(t, r);
-        o[j] = __fmul2_rn(t, q);
-      }
-      if (!FULL) {
-        o[0] = pick2(mk[i], mk[i + H], 0x000000ffu, o[0], cur[0]);
-        o[1] = pick2(mk[i], mk[i + H], 0x0000ff00u, o[1], cur[1]);
-        o[2] = pick2(mk[i], mk[i + H], 0x00ff0000u, o[2], cur[2]);
-        o[3] = pick2(mk[i], mk[i + H], 0xff000000u, o[3], cur[3]);
-      }
+      tbp_grad<R, GS>(Gp, sg, i, lane, gv);
+      tbp_update<R, FULL>(cur, up, dn, gv, mk, i, o);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         up[j] = cur[j];
         P[i][j] = o[j];
       }
     }
+  } else {
+    float2 dn[4] = {dlast[0], dlast[1], dlast[2], dlast[3]};
+#pragma unroll
+    for (int i = H - 1; i >= 0; --i) {
+      const float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
+      float2 up[4], gv[4], o[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) up[j] = i > 0 ? P[i - 1][j] : ufirst[j];
+      tbp_grad<R, GS>(Gp, sg, i, lane, gv);
+      tbp_update<R, FULL>(cur, up, dn, gv, mk, i, o);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        dn[j] = cur[j];
+        P[i][j] = o[j];
+      }
+    }
   }
+}
+
+// ksweeps packed sweeps of the strip held in P (pairs of rows i, i+R/2),
+// grad pairs in Gp (or shared memory sg when GS), mask words in mk:
+// forward/backward sweep pairs, then a last forward sweep if ksweeps is odd.
+// Sweep s uses edge buffer s & 1, so one barrier per sweep suffices.
+template <int R, int W, bool FULL, bool GS>
+__device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (&Gp)[GS ? 1 : R / 2][4],
+                                           const uint32_t (&mk)[R], int ksweeps, int lane, int w,
+                                           float4 (&edge)[2][2][W][32], const float2* __restrict__ sg) {
+  int s = 0;
+  for (; s + 2 <= ksweeps; s += 2) {
+    tbp_sweep<R, W, FULL, GS, true>(P, Gp, mk, 0, lane, w, edge, sg);
+    tbp_sweep<R, W, FULL, GS, false>(P, Gp, mk, 1, lane, w, edge, sg);
+  }
+  if (s < ksweeps) tbp_sweep<R, W, FULL, GS, true>(P, Gp, mk, 0, lane, w, edge, sg);
 }
 
 // TS: storage type of the swept state (float for the plain solver; __half

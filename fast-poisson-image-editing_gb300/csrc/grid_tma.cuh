@@ -19,11 +19,16 @@ void prepare_tma();
 // resident CTAs per SM).
 int tma_ctas(int items);
 
-// ksweeps (1..16) sweeps xin -> xout on every active tile, `ctas`
-// persistent CTAs.  A wait for a region copy that fails wait_limit polls
-// sets *error to 1 (the sweeps of that CTA are then incomplete).
+// Builds the active-tile list of `flags` (tiles + 1 ints: the count, then
+// the active tile indices in order); once per mask, before launch_tma.
+void launch_tma_list(const uint8_t* flags, int tiles, int* list, cudaStream_t st);
+
+// ksweeps (1..16) sweeps xin -> xout on every tile of `list`, `ctas`
+// persistent CTAs taking the (tile, channel) items round-robin.  A wait for
+// a region copy that fails wait_limit checks sets *error to 1 (the sweeps
+// of that CTA's remaining items are then missing).
 void launch_tma(const GridGeom& G, const uint8_t* mask, const float* g, const float* xin,
-                float* xout, const uint8_t* flags, int tiles_x, int tiles, int ksweeps,
-                int* error, long long wait_limit, int ctas, cudaStream_t st);
+                float* xout, const uint8_t* flags, const int* list, int tiles_x, int tiles,
+                int ksweeps, int* error, long long wait_limit, int ctas, cudaStream_t st);
 
 }  // namespace fpie
