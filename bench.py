@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import re
 import os
 import pathlib
 import statistics
@@ -90,6 +91,22 @@ def measured_peak():
         except Exception:
             pass
     return FALLBACK_HBM_GBS, "fallback"
+
+
+def kernel_shape(kernel: str, sweeps: int):
+    """(sweeps per launch, launches per step, region passes per launch) of a
+    grid sweep kernel, from its name: "sweep1"; "r/p<R>w<W>k<K>[s|t]" (K
+    sweeps per launch); "p16w8k16d" (dependency flow: the whole step in one
+    launch, a pass per 16-sweep level); "res16w8k4" (resident: the whole step
+    in one launch, one region load)."""
+    if kernel == "sweep1":
+        return 1, sweeps, 1
+    depth = int(re.search(r"k(\d+)", kernel).group(1))
+    if kernel.endswith("d"):
+        return sweeps, 1, -(-sweeps // depth)
+    if kernel.startswith("res"):
+        return sweeps, 1, 1
+    return depth, -(-sweeps // depth), 1
 
 
 def profiled_traffic(name: str):
@@ -352,15 +369,18 @@ def run_gb300(args):
 
     peak, peak_kind = measured_peak()
     kernel = s.kernel
-    depth = 1 if kernel == "sweep1" else int(kernel.split("k")[-1])
-    launches_per_step = -(-sweeps // depth)
+    per_launch, launches_per_step, passes = kernel_shape(kernel, sweeps)
     avg_launch_s = sweep_ms / 1e3 / (args.steps * launches_per_step)
     # Algorithmic bytes of one launch: 37 B per crop pixel per sweep, times
     # the sweeps one launch performs (the temporally blocked kernels do
-    # `depth` sweeps per launch on register-resident state).
-    alg_bytes = GRID_BYTES_PER_PX * crop_px * depth
+    # `depth` sweeps per launch on register-resident state; the flow and
+    # resident kernels a whole step).
+    alg_bytes = GRID_BYTES_PER_PX * crop_px * per_launch
     achieved = alg_bytes / avg_launch_s / 1e9
-    compulsory = GRID_BYTES_PER_PX * crop_px / avg_launch_s / 1e9
+    # Compulsory: one read of x/grad/mask and one write of x per pass over
+    # the regions (one per launch, or one per 16-sweep level of the flow
+    # kernel).
+    compulsory = GRID_BYTES_PER_PX * crop_px * passes / avg_launch_s / 1e9
 
     line = {
         "metric": "pixel-updates/s", "value": value, "unit": "pixel-updates/s", "n_gpus": world,
@@ -389,12 +409,13 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": profiled_traffic(f"grid_{kernel}_square800"),
-                     "kernel": kernel, "sweeps_per_launch": depth, "bytes_per_launch": alg_bytes,
+                     "kernel": kernel, "sweeps_per_launch": per_launch,
+                     "region_passes_per_launch": passes, "bytes_per_launch": alg_bytes,
                      "avg_launch_us": avg_launch_s * 1e6, "peak_source": f"hbm_gbs ({peak_kind})",
                      "compulsory_gbs": compulsory, "compulsory_frac": compulsory / peak,
                      "note": "achieved counts 37 B/pixel for every sweep a launch performs; "
                              "compulsory counts one read of x/grad/mask and one write of x "
-                             "per launch"},
+                             "per pass over the regions"},
         "clocks": clk,
         "parity": {"timed_output_equals_fresh_solve": same},
     }

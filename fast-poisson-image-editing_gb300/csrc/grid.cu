@@ -19,6 +19,7 @@
 #include "grid_kernels.cuh"
 #include "grid_mixed.cuh"
 #include "grid_resident.cuh"
+#include "grid_flow.cuh"
 #include "grid_tma.cuh"
 #include "grid_tb.cuh"
 
@@ -135,6 +136,15 @@ struct GridSolverImpl : Solver {
   int tma_list_cap = 0;
   int tma_grid = 0;          // persistent CTAs for the current tiling
 
+  // ---- dependency-flow kernel (variant index kFlow) ---------------------------
+  // Shares the active-tile list and the wait-error flag with the TMA kernel.
+  static constexpr int kFlow = -4;
+  int* flow_inv = nullptr;   // tile -> active-list index
+  void* flow_rec = nullptr;  // per active tile: index, flag, neighbourhood
+  int* flow_done = nullptr;  // levels finished per (active tile, channel)
+  int flow_cap = 0;          // tiles the two arrays hold
+  int flow_grid = 0;
+
   // Reads and clears the TMA kernel's time-out flag; call after the stream
   // has been synchronised.
   void check_tma() {
@@ -221,6 +231,18 @@ struct GridSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(r_nbrs, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
     return true;
+  }
+
+  // All `iters` sweeps in one launch of the dependency-flow kernel.  A wait
+  // that timed out is reported at the next host synchronisation.
+  void run_flow(int iters) {
+    ensure_flags();
+    FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)tiles * 3 * sizeof(int), stream));
+    launch_flow(G, mask, g, x[0], x[1], cur, tma_list, flow_rec, flow_done, tiles_x, tiles, iters,
+                d_tma_err, r_spin_limit, flow_grid, stream);
+    post_launch(this);
+    const int levels = (iters + flow_depth() - 1) / flow_depth();
+    if (levels & 1) cur ^= 1;
   }
 
   // All `iters` sweeps in one cooperative launch.
@@ -319,6 +341,13 @@ struct GridSolverImpl : Solver {
     release_resident();
     cudaFree(d_tma_err);
     cudaFree(tma_list);
+    cudaFree(flow_inv);
+    cudaFree(flow_done);
+    cudaFree(flow_rec);
+    flow_inv = nullptr;
+    flow_done = nullptr;
+    flow_rec = nullptr;
+    flow_cap = 0;
     if (h_tma_err) cudaFreeHost(h_tma_err);
     d_tma_err = nullptr;
     h_tma_err = nullptr;
@@ -504,15 +533,18 @@ struct GridSolverImpl : Solver {
 
   int depth() const {
     if (variant == kTma) return tma_depth();
+    if (variant == kFlow) return flow_depth();
     return variant < 0 ? 1 : tb_variants()[variant].depth;
   }
 
   void ensure_flags() {
-    if (flags_ok || (variant < 0 && variant != kTma)) return;  // sweep1 / resident: no flags
-    const bool tma = variant == kTma;
-    const int th = tma ? tma_tile_h() : tb_variants()[variant].tile_h;
-    const int tw = tma ? tma_tile_w() : tb_variants()[variant].tile_w;
-    const int kd = tma ? tma_depth() : tb_variants()[variant].depth;
+    // sweep1 / resident: no flags
+    if (flags_ok || (variant < 0 && variant != kTma && variant != kFlow)) return;
+    const bool tma = variant == kTma, flow = variant == kFlow;
+    const bool listed = tma || flow;  // kernels that take the active-tile list
+    const int th = tma ? tma_tile_h() : flow ? flow_tile_h() : tb_variants()[variant].tile_h;
+    const int tw = tma ? tma_tile_w() : flow ? flow_tile_w() : tb_variants()[variant].tile_w;
+    const int kd = tma ? tma_depth() : flow ? flow_depth() : tb_variants()[variant].depth;
     tiles_x = (G.m + tw - 1) / tw;
     tiles = tiles_x * ((G.n + th - 1) / th);
     if (tiles > flags_cap) {
@@ -521,9 +553,24 @@ struct GridSolverImpl : Solver {
       FPIE_CUDA(cudaMalloc(&flags, tiles));
       flags_cap = tiles;
     }
-    if (tma) {
-      prepare_tma();
-      tma_grid = tma_ctas(tiles * 3);
+    if (listed) {
+      if (tma) {
+        prepare_tma();
+        tma_grid = tma_ctas(tiles * 3);
+      } else {
+        flow_grid = flow_ctas();
+        if (tiles > flow_cap) {
+          cudaFree(flow_inv);
+          cudaFree(flow_done);
+          cudaFree(flow_rec);
+          flow_inv = flow_done = nullptr;
+          flow_rec = nullptr;
+          FPIE_CUDA(cudaMalloc(&flow_inv, (size_t)tiles * sizeof(int)));
+          FPIE_CUDA(cudaMalloc(&flow_done, (size_t)tiles * 3 * sizeof(int)));
+          FPIE_CUDA(cudaMalloc(&flow_rec, (size_t)tiles * flow_rec_bytes()));
+          flow_cap = tiles;
+        }
+      }
       if (!d_tma_err) {
         FPIE_CUDA(cudaMalloc(&d_tma_err, sizeof(int)));
         FPIE_CUDA(cudaMallocHost(&h_tma_err, sizeof(int)));
@@ -541,8 +588,12 @@ struct GridSolverImpl : Solver {
     }
     launch_tile_flags(G, mask, th, tw, kd, tiles_x, tiles, flags, stream);
     post_launch(this);
-    if (tma) {
+    if (listed) {
       launch_tma_list(flags, tiles, tma_list, stream);
+      post_launch(this);
+    }
+    if (flow) {
+      launch_flow_tables(tma_list, flags, tiles_x, tiles, flow_inv, flow_rec, stream);
       post_launch(this);
     }
     flags_ok = true;
@@ -647,6 +698,28 @@ struct GridSolverImpl : Solver {
         }
       }
     }
+    // The dependency-flow kernel runs a whole step per launch; timed on 4
+    // chunks per launch so that its start and end (one level each) weigh as
+    // little as in a real step.
+    if (iters - used >= (kTuneReps + 1) * 4 * kChunk) {
+      select_variant(kFlow);
+      run_flow(4 * kChunk);
+      used += 4 * kChunk;
+      for (int r = 0; r < kTuneReps; ++r) {
+        FPIE_CUDA(cudaEventRecord(e0, stream));
+        run_flow(4 * kChunk);
+        FPIE_CUDA(cudaEventRecord(e1, stream));
+        FPIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        used += 4 * kChunk;
+        if (ms / 4 < best_ms) {
+          best_ms = ms / 4;
+          best = kFlow;
+        }
+      }
+      check_tma();
+    }
     // The resident kernel, when every active tile fits co-resident.
     if (build_resident() && r_nctas > 0 && iters - used >= (kTuneReps + 1) * kChunk) {
       select_variant(kResident);
@@ -685,6 +758,10 @@ struct GridSolverImpl : Solver {
     if (!tuned && !pinned) iters -= autotune(iters);
     if (variant == kResident) {
       if (iters > 0) run_resident(iters);
+      return;
+    }
+    if (variant == kFlow) {
+      if (iters > 0) run_flow(iters);
       return;
     }
     while (iters >= kChunk) {
@@ -942,6 +1019,7 @@ struct GridSolverImpl : Solver {
     if (name == "sweep1") v = -1;
     if (name == "res16w8k4") v = kResident;
     if (name == "p16w8k16t") v = kTma;
+    if (name == "p16w8k16d") v = kFlow;
     for (size_t k = 0; k < tb_variants().size(); ++k)
       if (name == tb_variants()[k].name) v = (int)k;
     FPIE_REQUIRE(v != -100, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
@@ -953,6 +1031,7 @@ struct GridSolverImpl : Solver {
     if (precision != FPIE_FP32) return std::string(mixed_variants()[mvariant].name);
     if (variant == kResident) return std::string("res16w8k4");
     if (variant == kTma) return std::string("p16w8k16t");
+    if (variant == kFlow) return std::string("p16w8k16d");
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }
 

@@ -1,0 +1,237 @@
+// Dependency-flow grid sweep ("p16w8k16d"): a whole step in one launch.
+//
+// The sweeps are cut into levels of up to 16 (the packed variant
+// p16w8k16's temporal depth: 96x96 tiles in 128x128 register-resident
+// regions, same arithmetic, bit-identical results).  A work item is one
+// (level, active tile, channel); items are numbered level-major and CTA b
+// of a cooperative launch takes items b, b + gridDim.x, ...  Item
+// (z, tile, c) reads buffer (p + z) & 1 over its region and writes the tile
+// interior to buffer (p + z + 1) & 1.  It may start once every active tile
+// of its 3x3 neighbourhood (same channel, itself included) has finished
+// level z - 1, which covers both hazards on the ping-pong buffers:
+//   - read after write: the region (tile + 16-pixel apron) lies inside the
+//     neighbourhood, whose level z - 1 outputs are then complete;
+//   - write after read: the buffer being written was read at level z - 1
+//     only by items of the neighbourhood, which are then finished.
+// Inactive tiles (no masked pixel) never change and hold the same values
+// in both buffers, so nobody waits for them.
+//
+// A CTA never waits for a later-numbered item, and all CTAs of a
+// cooperative launch are co-resident, so the waits always end; they are
+// bounded anyway (the solver's spin limit): past it the CTA records an
+// error, every CTA stops at its next wait, and the host reports
+// FPIE_ERR_TIMEOUT.
+//
+// What this buys over one launch per 16 sweeps: no launch gaps, and no
+// wave tail -- when a level has, say, 243 items on 152 SMs, CTAs that are
+// done with their level-z items go on to level z + 1 items whose
+// neighbourhoods are ready instead of idling until the whole level ends.
+#include <algorithm>
+
+#include "common.cuh"
+#include "grid_flow.cuh"
+#include "grid_tbp.cuh"
+
+namespace fpie {
+
+namespace {
+
+constexpr int kR = 16, kW = 8, kK = 16;
+constexpr int kTH = kW * kR - 2 * kK;  // 96
+constexpr int kTW = 128 - 2 * kK;      // 96
+
+// Per active tile: {tile, flag, nb[0..8]} with nb = 3 x (active-list index)
+// of each tile of the 3x3 neighbourhood (row-major, itself at 4), -1 where
+// there is no active tile; padded to 12 ints (three int4 loads).
+struct FlowRec {
+  int tile, flag, nb[9], pad;
+};
+static_assert(sizeof(FlowRec) == 48, "three int4");
+
+struct FlowArgs {
+  GridGeom G;
+  const uint8_t* mask;
+  const float* g;
+  float* x[2];
+  const int* list;       // active tiles in tile order; list[-1] = their count
+  const FlowRec* rec;    // per active tile
+  int* done;             // per (active tile, channel): levels finished
+  int* error;
+  int tiles_x, sweeps, parity;
+  long long spin_limit;
+};
+
+__device__ __forceinline__ FlowRec load_rec(const FlowRec* r) {
+  const int4* q = reinterpret_cast<const int4*>(r);
+  const int4 a = q[0], b = q[1], d = q[2];
+  return FlowRec{a.x, a.y, {a.z, a.w, b.x, b.y, b.z, b.w, d.x, d.y, d.z}, d.w};
+}
+
+// The nine neighbourhood counters of channel c (INT_MAX where none).
+__device__ __forceinline__ void load_counters(const FlowArgs& A, const FlowRec& R, int c,
+                                              int (&v)[9]) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    v[k] = R.nb[k] >= 0 ? *(const volatile int*)(A.done + R.nb[k] + c) : 0x7fffffff;
+}
+
+__device__ __forceinline__ bool counters_reach(const int (&v)[9], int level) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) ok = ok && v[k] >= level;
+  return ok;
+}
+
+// Thread 0: waits until the counters in v (loaded earlier, possibly stale --
+// counters only grow) all reach `level`, reloading them together each round.
+// False if the wait gave up or another CTA did.
+__device__ __forceinline__ bool wait_counters(const FlowArgs& A, const FlowRec& R, int c,
+                                              int level, int (&v)[9]) {
+  for (long long spins = 0; !counters_reach(v, level); ++spins) {
+    if (*(volatile int*)A.error) return false;
+    if (spins >= A.spin_limit) {
+      atomicExch(A.error, 1);
+      return false;
+    }
+    __nanosleep(64);
+    load_counters(A, R, c, v);
+  }
+  return true;
+}
+
+// One item, out of line: inlined into the item loop, the compiler's register
+// assignment needs several times the register moves per sweep of the same
+// code in the launch-per-tile kernel (measured by instruction counters).
+template <bool FULL>
+__device__ __noinline__ void flow_item(const FlowArgs& A, int tile, int c, int z,
+                                       float4 (&edge)[2][2][kW][32], int lane, int w) {
+  const GridGeom& G = A.G;
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long co = c * G.plane;
+  const int pin = (A.parity + z) & 1;
+  const int ks = min(kK, A.sweeps - z * kK);
+  // CG: the state is read through L2, since other CTAs wrote it during
+  // this launch.
+  tbp_body<kR, kW, kK, FULL, float, false, true>(G, A.mask, A.g + co, A.x[pin] + co,
+                                                 A.x[pin ^ 1] + co, base, ks, lane, w, edge);
+}
+
+// Thread 0 keeps the next item's record and counters, loaded right after
+// the current item's sweeps so that their latency overlaps the release
+// fence and barrier; the other threads get tile and flag through shared
+// memory.
+__global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
+  __shared__ float4 edge[2][2][kW][32];
+  __shared__ int s_stop, s_tile, s_flag;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int per = 3 * A.list[-1];
+  const int levels = (A.sweeps + kK - 1) / kK;
+  const long long total = (long long)levels * per;
+  FlowRec R{};
+  int v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (threadIdx.x == 0 && blockIdx.x < total) {
+    const int r = (int)blockIdx.x % per;
+    R = load_rec(A.rec + r / 3);
+    load_counters(A, R, r % 3, v);
+  }
+  for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
+    const int z = (int)(idx / per), r = (int)(idx - (long long)z * per);
+    const int a = r / 3, c = r - 3 * a;
+    if (threadIdx.x == 0) {
+      const bool ok = z == 0 || wait_counters(A, R, c, z, v);
+      __threadfence();  // acquire: the neighbours' writes before our reads
+      s_stop = !ok;
+      s_tile = R.tile;
+      s_flag = R.flag;
+    }
+    __syncthreads();
+    if (s_stop) break;
+    const int tile = s_tile;
+    if (s_flag == 2)
+      flow_item<true>(A, tile, c, z, edge, lane, w);
+    else
+      flow_item<false>(A, tile, c, z, edge, lane, w);
+    const long long next = idx + gridDim.x;
+    if (threadIdx.x == 0 && next < total) {
+      const int rn = (int)(next % per);
+      R = load_rec(A.rec + rn / 3);
+      load_counters(A, R, rn % 3, v);
+    }
+    // Release, as a grid-wide barrier does it: the CTA barrier orders every
+    // thread's writes before thread 0's fence, which orders them before the
+    // counter update.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(A.done + 3 * a + c, 1);
+    }
+  }
+}
+
+// inv[t] = index of tile t in the active list, -1 for inactive tiles.
+__global__ void flow_inv_kernel(const int* __restrict__ list, int tiles, int* __restrict__ inv) {
+  const int n = list[-1];
+  for (int t = threadIdx.x; t < tiles; t += blockDim.x) inv[t] = -1;
+  __syncthreads();  // one block: the -1 fill precedes the scatter
+  for (int a = threadIdx.x; a < n; a += blockDim.x) inv[list[a]] = a;
+}
+
+__global__ void flow_rec_kernel(const int* __restrict__ list, const int* __restrict__ inv,
+                                const uint8_t* __restrict__ flags, int tiles_x, int tiles_y,
+                                FlowRec* __restrict__ rec) {
+  const int n = list[-1];
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const int tile = list[a], ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    FlowRec R;
+    R.tile = tile;
+    R.flag = flags[tile];
+    R.pad = 0;
+    for (int k = 0; k < 9; ++k) {
+      const int y = ty + k / 3 - 1, x = tx + k % 3 - 1;
+      const int b = (y >= 0 && y < tiles_y && x >= 0 && x < tiles_x) ? inv[y * tiles_x + x] : -1;
+      R.nb[k] = b >= 0 ? 3 * b : -1;
+    }
+    rec[a] = R;
+  }
+}
+
+}  // namespace
+
+int flow_tile_h() { return kTH; }
+int flow_tile_w() { return kTW; }
+int flow_depth() { return kK; }
+
+int flow_ctas() {
+  int dev = 0, sms = 0, per_sm = 0;
+  FPIE_CUDA(cudaGetDevice(&dev));
+  FPIE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_flow_kernel, kW * 32, 0));
+  FPIE_REQUIRE(per_sm >= 1, FPIE_ERR_CUDA, "the flow sweep kernel does not fit on an SM");
+  return sms * per_sm;
+}
+
+void launch_flow_tables(const int* list, const uint8_t* flags, int tiles_x, int tiles, int* inv,
+                        void* rec, cudaStream_t st) {
+  flow_inv_kernel<<<1, 1024, 0, st>>>(list + 1, tiles, inv);
+  flow_rec_kernel<<<(tiles + 255) / 256, 256, 0, st>>>(list + 1, inv, flags, tiles_x,
+                                                       tiles / tiles_x,
+                                                       static_cast<FlowRec*>(rec));
+}
+
+size_t flow_rec_bytes() { return sizeof(FlowRec); }
+
+void launch_flow(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
+                 int parity, const int* list, const void* rec, int* done, int tiles_x, int tiles,
+                 int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st) {
+  FPIE_REQUIRE(sweeps >= 1, FPIE_ERR_ARG, "flow sweep kernel: at least one sweep");
+  FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
+               "flow sweep kernel: bad tiling");
+  FlowArgs a{G, mask, g, {x0, x1}, list + 1, static_cast<const FlowRec*>(rec), done, error,
+             tiles_x, sweeps, parity & 1, spin_limit};
+  void* args[] = {&a};
+  FPIE_CUDA(cudaLaunchCooperativeKernel((const void*)grid_flow_kernel, dim3(ctas), dim3(kW * 32),
+                                        args, 0, st));
+}
+
+}  // namespace fpie

@@ -127,7 +127,7 @@ def test_tensor_handoff(backend):
 
 KERNELS = ["sweep1", "r8w8k8", "r16w8k8", "r8w16k8", "r16w8k16", "r8w16k16", "r16w10k8s",
            "r16w12k8s", "r12w16k16s", "p16w8k8", "p16w8k16", "p8w16k16", "p8w12k8",
-           "p16w8k4", "p12w12k8s", "p8w16k8s", "res16w8k4", "p16w8k16t"]
+           "p16w8k4", "p12w12k8s", "p8w16k8s", "res16w8k4", "p16w8k16t", "p16w8k16d"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -235,10 +235,14 @@ def _many_items_case():
     return mask, tgt, grad
 
 
-def test_tma_kernel_many_items_per_cta(backend):
+@pytest.mark.parametrize("kernel", ["p16w8k16t", "p16w8k16d"])
+def test_persistent_kernels_many_items_per_cta(backend, kernel):
+    """The persistent kernels (TMA prefetch; dependency flow, whose CTAs run
+    ahead into the next level where neighbourhoods are ready) on a grid with
+    several items per CTA, against the oracle."""
     mask, tgt, grad = _many_items_case()
     s = backend.GridSolver(8, 8)
-    s.set_kernel("p16w8k16t")
+    s.set_kernel(kernel)
     s.reset(mask.size, mask, tgt, grad)
     o = cjacobi.CGrid(mask, tgt, grad)
     for k in (1, 15, 130):  # a 1-sweep launch, a partial block, graph chunks
@@ -261,6 +265,27 @@ def test_tma_wait_times_out_without_hanging(backend):
     s.reset(mc.size, mc, t, g)
     with pytest.raises(_abi.FpieTimeoutError):
         s.step(64)
+    s.set_spin_limit(1 << 26)
+    s.reset(mc.size, mc, t, g)
+    s.step(100)
+    o = cjacobi.CGrid(mc, t, g)
+    o.sweep(100)
+    np.testing.assert_array_equal(s.state(), o.x)
+
+
+def test_flow_wait_times_out_without_hanging(backend):
+    """Spin limit 0: a neighbourhood wait of the dependency-flow kernel gives
+    up at its first unmet check; the launch stops, the next synchronising
+    call raises the timeout, and the solver and GPU stay usable."""
+    from fpie_gb300 import _abi
+
+    mc, t, g, _ = _square800_grid()
+    s = backend.GridSolver(8, 8)
+    s.set_kernel("p16w8k16d")
+    s.set_spin_limit(0)
+    s.reset(mc.size, mc, t, g)
+    with pytest.raises(_abi.FpieTimeoutError):
+        s.step(5000)
     s.set_spin_limit(1 << 26)
     s.reset(mc.size, mc, t, g)
     s.step(100)
