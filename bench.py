@@ -454,8 +454,12 @@ def run_gb300(args):
         q_ms = sum(a for a, _ in qt)
         q_sweep = sum(b for _, b in qt) / 1e3 / (qsteps * sweeps)
         line["equ"] = {"value": (sysm.N - 1) * sweeps * qsteps / (q_ms / 1e3), "unit": "pixel-updates/s",
-                       "ms_per_step": q_ms / qsteps, "steps": qsteps,
-                       "sweep_kernel_achieved_gbs": EQU_BYTES_PER_UNKNOWN * sysm.N / q_sweep / 1e9}
+                       "ms_per_step": q_ms / qsteps, "steps": qsteps, "kernel": q.kernel,
+                       "sweep_kernel_achieved_gbs": EQU_BYTES_PER_UNKNOWN * sysm.N / q_sweep / 1e9,
+                       "note": "reset_tensors (A/X/B from HBM; the placement on a grid is "
+                               "re-checked on the device) + 5000 sweeps + residual + uint8 "
+                               "values; 'grid:<k>' = the system is a 4-neighbour raster "
+                               "stencil swept by grid kernel k"}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_grid(mc, t, g)

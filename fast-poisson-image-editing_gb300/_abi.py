@@ -68,6 +68,10 @@ _PROTOS: dict[str, tuple] = {
                                _I, _P, ctypes.POINTER(_I)], _I),
     "fpie_equ_get_index": ([_P, _P, _P], _I),
     "fpie_equ_get_inputs": ([_P, _P, _P], _I),
+    "fpie_equ_set_kernel": ([_P, ctypes.c_char_p], _I),
+    "fpie_equ_kernel": ([_P, ctypes.c_char_p, _I], _I),
+    "fpie_equ_set_spin_limit": ([_P, ctypes.c_longlong], _I),
+    "fpie_equ_raster_layout": ([_I, _P, _P, _P, _P], _I),
     "fpie_batch_create": ([ctypes.c_double, ctypes.POINTER(_P)], _I),
     "fpie_batch_destroy": ([_P], _I),
     "fpie_batch_job_bytes": ([_I, _I, ctypes.POINTER(ctypes.c_double)], _I),

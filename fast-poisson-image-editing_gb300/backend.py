@@ -124,6 +124,21 @@ class _Solver:
         return c.value
 
 
+def raster_layout(A: np.ndarray):
+    """Placement of a 4-neighbour raster equation system on a grid (host only).
+
+    Returns (pos int32[N], (n, m)) -- pos[i] = row * m + col of unknown i,
+    pos[0] = -1 -- or None when A is not a raster stencil."""
+    A = _as(A, np.int32, (None, 4), "A")
+    pos = np.empty(A.shape[0], np.int32)
+    n, m = ctypes.c_int(0), ctypes.c_int(0)
+    rc = _abi.lib().fpie_equ_raster_layout(A.shape[0], _ptr(A), _ptr(pos), ctypes.byref(n),
+                                           ctypes.byref(m))
+    if rc != 0:
+        return None
+    return pos, (n.value, m.value)
+
+
 class EquSolver(_Solver):
     """Jacobi on relabelled unknowns (fpie/core/base_solver.h:12-75)."""
 
@@ -171,6 +186,22 @@ class EquSolver(_Solver):
         if self.N > 1:
             _abi.call("fpie_equ_get_index", self._h, _ptr(rows), _ptr(cols))
         return self.N, tuple(box), (rows.astype(np.int64), cols.astype(np.int64))
+
+    def set_kernel(self, name: str) -> None:
+        """"auto" (grid kernels for 4-neighbour raster systems, else gather),
+        "gather", or a grid kernel name; applies from the next reset."""
+        _abi.call("fpie_equ_set_kernel", self._h, name.encode())
+
+    @property
+    def kernel(self) -> str:
+        """"gather" or "grid:<grid kernel>"."""
+        buf = ctypes.create_string_buffer(64)
+        _abi.call("fpie_equ_kernel", self._h, buf, 64)
+        return buf.value.decode()
+
+    def set_spin_limit(self, spins: int) -> None:
+        """Bounded-wait limit of the grid kernels used in grid placement."""
+        _abi.call("fpie_equ_set_spin_limit", self._h, ctypes.c_longlong(int(spins)))
 
     def inputs(self) -> tuple[np.ndarray, np.ndarray]:
         """(A int32[N,4], B float32[N,3]) as the solver holds them."""

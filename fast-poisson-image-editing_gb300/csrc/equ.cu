@@ -7,7 +7,9 @@
 // channel arrays, a deterministic residual reduction, checked CUDA calls,
 // and neighbour indices validated before any kernel reads through them.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -121,6 +123,128 @@ static int conv_blocks(long long total) {
   return (int)std::max<long long>(1, std::min<long long>(b, 152 * 32));
 }
 
+Solver* new_grid_solver(int grid_x, int grid_y);
+void grid_reset_from_equ(Solver* s, cudaStream_t st, int n, int m, int N, const int* pos,
+                         const float* xe, const float* be, long long np);
+void grid_to_equ(Solver* s, cudaStream_t st, int N, const int* pos, float* xe, long long np);
+void grid_run(Solver* s, cudaStream_t st, int iters);
+void grid_pin_kernel(Solver* s, const std::string& name);
+std::string grid_kernel_of(Solver* s);
+void grid_set_spin(Solver* s, long long spins);
+
+// Whether the system A (N x 4: up, down, left, right; 0 = the constant row)
+// is a 4-neighbour raster stencil, i.e. its unknowns can be placed on a grid
+// so that each one's grid neighbours are exactly its A entries (0 where the
+// grid pixel holds no unknown).  EquProcessor builds such systems from a
+// mask (fpie/process.py:253-265); then the equation sweep
+// X' = ((((B + X[U]) + X[D]) + X[L]) + X[R]) / 4 is, operation for
+// operation, the grid sweep with grad = B and 0 at every pixel that is not
+// an unknown.  On success pos[i] (i >= 1) is unknown i's pixel, row-major in
+// an n x m crop: connected components are placed one below the other, a row
+// apart, inside a 1-pixel frame.  Row 0 must be the constant (all-zero A).
+static bool raster_embed(int N, const int32_t* A, std::vector<int>& pos, int& n, int& m) {
+  if (N < 2) return false;
+  for (int k = 0; k < 4; ++k)
+    if (A[k] != 0) return false;
+  static const int dr[4] = {-1, 1, 0, 0}, dc[4] = {0, 0, -1, 1};
+  std::vector<int> R(N, 0), C(N, 0);
+  std::vector<char> seen(N, 0);
+  std::vector<int> queue;
+  queue.reserve(N);
+  long long rows = 1;  // the top frame row
+  long long width = 0;
+  for (int s = 1; s < N; ++s) {
+    if (seen[s]) continue;
+    const size_t head = queue.size();
+    queue.push_back(s);
+    seen[s] = 1;
+    int rmin = 0, rmax = 0, cmin = 0, cmax = 0;
+    for (size_t q = head; q < queue.size(); ++q) {
+      const int i = queue[q];
+      for (int k = 0; k < 4; ++k) {
+        const int j = A[4 * (size_t)i + k];
+        if (j == 0) continue;
+        if (j < 0 || j >= N) return false;
+        const int rj = R[i] + dr[k], cj = C[i] + dc[k];
+        if (!seen[j]) {
+          seen[j] = 1;
+          R[j] = rj;
+          C[j] = cj;
+          rmin = std::min(rmin, rj);
+          rmax = std::max(rmax, rj);
+          cmin = std::min(cmin, cj);
+          cmax = std::max(cmax, cj);
+          queue.push_back(j);
+        } else if (R[j] != rj || C[j] != cj) {
+          return false;
+        }
+      }
+    }
+    for (size_t q = head; q < queue.size(); ++q) {
+      R[queue[q]] += (int)(rows - rmin);
+      C[queue[q]] += 1 - cmin;
+    }
+    rows += (long long)(rmax - rmin + 1) + 1;  // the component, then an empty row
+    width = std::max(width, (long long)(cmax - cmin + 1) + 2);
+    if (rows > (1LL << 30)) return false;
+  }
+  // The crop must stay comparable to the system (many scattered pieces would
+  // make a mostly empty grid; the gather kernel is better there).
+  if (rows * width > 8LL * N + (1LL << 20) || rows * width > (1LL << 31) / 4) return false;
+  n = (int)rows;
+  m = (int)width;
+  std::vector<int> occ((size_t)n * m, 0);
+  for (int i = 1; i < N; ++i) {
+    int& o = occ[(size_t)R[i] * m + C[i]];
+    if (o) return false;  // two unknowns on one pixel
+    o = i;
+  }
+  for (int i = 1; i < N; ++i)
+    for (int k = 0; k < 4; ++k)
+      if (occ[(size_t)(R[i] + dr[k]) * m + (C[i] + dc[k])] != A[4 * (size_t)i + k]) return false;
+  pos.assign(N, 0);
+  for (int i = 1; i < N; ++i) pos[i] = R[i] * m + C[i];
+  return true;
+}
+
+// Pixels of the unknowns from their target coordinates (the GPU-side reset
+// knows them): pos[i] = (rows[i-1] - r0) * m + (cols[i-1] - c0).
+__global__ void equ_pos_kernel(int N, const int* __restrict__ rows, const int* __restrict__ cols,
+                               int r0, int c0, int m, int* __restrict__ pos) {
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    pos[i] = (rows[i - 1] - r0) * m + (cols[i - 1] - c0);
+}
+
+// Counts violations of a cached placement (pos, occ: unknown id per crop
+// pixel, 0 elsewhere; m pixels per row) by the system now in A / x / b:
+// row 0 must be the zero constant, and every unknown's four grid neighbours
+// must be exactly its A entries -- the condition raster_embed establishes.
+__global__ void equ_layout_check_kernel(EquGeom E, const int4* __restrict__ A,
+                                        const float* __restrict__ x, const float* __restrict__ b,
+                                        const int* __restrict__ pos, const int* __restrict__ occ,
+                                        int m, unsigned int* __restrict__ bad) {
+  unsigned int nbad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < E.N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int4 a = A[i];
+    if (i == 0) {
+      nbad += (a.x | a.y | a.z | a.w) != 0;
+      for (int c = 0; c < 3; ++c) nbad += (x[c * E.np] != 0.f) + (b[c * E.np] != 0.f);
+      continue;
+    }
+    const int p = pos[i];
+    nbad += (occ[p - m] != a.x) + (occ[p + m] != a.y) + (occ[p - 1] != a.z) + (occ[p + 1] != a.w);
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+__global__ void equ_occ_kernel(int N, const int* __restrict__ pos, int* __restrict__ occ) {
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    occ[pos[i]] = (int)i;
+}
+
 struct EquSolverImpl : Solver {
   int block = 256;
   bool ready = false;
@@ -140,6 +264,21 @@ struct EquSolverImpl : Solver {
   static constexpr int kChunk = 64;
   cudaGraphExec_t chunk[2] = {nullptr, nullptr};
 
+  // ---- grid mode: systems that are a 4-neighbour raster stencil run on an
+  // internal grid solver (its autotuned temporally blocked kernels); the
+  // state lives there and is gathered back into x[cur] when needed.
+  std::string kernel_req = "auto";  // "auto" | "gather" | a grid kernel name
+  Solver* grid = nullptr;
+  int* d_pos = nullptr;             // per unknown: its crop pixel
+  int pos_cap = 0;
+  bool use_grid = false;
+  bool grid_newer = false;          // grid state ahead of x[cur]
+  // The last placement found by the host search, kept to be re-checked on
+  // the device at the next reset of a system of the same size.
+  int* d_occ = nullptr;             // unknown id per crop pixel
+  int lay_N = 0, lay_n = 0, lay_m = 0;
+  long long spin_limit = 1LL << 26;
+
   explicit EquSolverImpl(int block_size) {
     kind = 1;
     if (block_size >= 32 && block_size <= 1024 && block_size % 32 == 0) block = block_size;
@@ -153,6 +292,9 @@ struct EquSolverImpl : Solver {
 
   ~EquSolverImpl() override {
     release();
+    delete grid;
+    cudaFree(d_pos);
+    cudaFree(d_occ);
     cudaFree(d_rows);
     cudaFree(d_cols);
     cudaFree(d_bad);
@@ -186,6 +328,113 @@ struct EquSolverImpl : Solver {
     d_err = nullptr;
     h_img = nullptr;
     ready = false;
+    use_grid = false;
+    grid_newer = false;
+  }
+
+  void ensure_pos(int N) {
+    if (N > pos_cap) {
+      cudaFree(d_pos);
+      d_pos = nullptr;
+      FPIE_CUDA(cudaMalloc(&d_pos, sizeof(int) * (size_t)N));
+      pos_cap = N;
+    }
+  }
+
+  // Moves the system into grid mode at crop size n x m (d_pos filled).
+  void enter_grid(int n, int m) {
+    if (!grid) grid = new_grid_solver(8, 8);
+    grid_set_spin(grid, spin_limit);
+    if (kernel_req != "auto") grid_pin_kernel(grid, kernel_req);
+    grid_reset_from_equ(grid, stream, n, m, E.N, d_pos, x[0], b, E.np);
+    use_grid = true;
+    grid_newer = false;
+  }
+
+  // Whether the last placement fits the system now loaded (device check).
+  bool cached_layout_fits() {
+    if (!d_occ || lay_N != E.N || lay_N < 2) return false;
+    FPIE_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), stream));
+    equ_layout_check_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, A, x[0], b, d_pos, d_occ,
+                                                                   lay_m, d_bad);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(h_bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    return *h_bad == 0;
+  }
+
+  // After a reset from host or device arrays: grid mode when the system is
+  // a raster stencil (and the kernel choice allows it).  hA: the system's A
+  // on the host, or NULL to fetch it from the device if the search is needed.
+  void choose_mode(const int32_t* hA) {
+    use_grid = false;
+    if (kernel_req == "gather") return;
+    if (cached_layout_fits()) {
+      enter_grid(lay_n, lay_m);
+      return;
+    }
+    std::vector<int32_t> fetched;
+    if (!hA) {
+      fetched.resize((size_t)E.N * 4);
+      FPIE_CUDA(cudaMemcpyAsync(fetched.data(), A, (size_t)E.N * 16, cudaMemcpyDeviceToHost, stream));
+      FPIE_CUDA(cudaStreamSynchronize(stream));
+      hA = fetched.data();
+    }
+    float row0[6];
+    for (int c = 0; c < 3; ++c) {
+      FPIE_CUDA(cudaMemcpyAsync(row0 + c, x[0] + c * E.np, 4, cudaMemcpyDeviceToHost, stream));
+      FPIE_CUDA(cudaMemcpyAsync(row0 + 3 + c, b + c * E.np, 4, cudaMemcpyDeviceToHost, stream));
+    }
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    bool zero_row0 = true;
+    for (float v : row0) zero_row0 = zero_row0 && v == 0.f;
+    std::vector<int> pos;
+    int n = 0, m = 0;
+    const bool ok = zero_row0 && raster_embed(E.N, hA, pos, n, m);
+    if (!ok) {
+      FPIE_REQUIRE(kernel_req == "auto", FPIE_ERR_ARG,
+                   "grid kernel '" + kernel_req + "' needs a 4-neighbour raster system "
+                   "(row 0 constant and zero; every unknown's up/down/left/right in A)");
+      return;
+    }
+    ensure_pos(E.N);
+    FPIE_CUDA(cudaMemcpyAsync(d_pos, pos.data(), sizeof(int) * (size_t)E.N, cudaMemcpyHostToDevice,
+                              stream));
+    cudaFree(d_occ);
+    d_occ = nullptr;
+    lay_N = 0;
+    FPIE_CUDA(cudaMalloc(&d_occ, sizeof(int) * (size_t)n * m));
+    FPIE_CUDA(cudaMemsetAsync(d_occ, 0, sizeof(int) * (size_t)n * m, stream));
+    equ_occ_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E.N, d_pos, d_occ);
+    post_launch(this);
+    lay_N = E.N;
+    lay_n = n;
+    lay_m = m;
+    enter_grid(n, m);
+    FPIE_CUDA(cudaStreamSynchronize(stream));  // pos is a host vector
+  }
+
+  // x[cur] up to date with the grid state.
+  void sync_from_grid() {
+    if (use_grid && grid_newer) {
+      grid_to_equ(grid, stream, E.N, d_pos, x[cur], E.np);
+      grid_newer = false;
+    }
+  }
+
+  void check_async() override {
+    if (grid) grid->check_async();
+  }
+
+  void set_kernel(const std::string& name) {
+    kernel_req = name;
+    if (grid && name != "auto" && name != "gather") grid_pin_kernel(grid, name);
+    if (grid && name == "auto") grid_pin_kernel(grid, "auto");
+  }
+
+  std::string kernel_name() const {
+    if (!use_grid) return "gather";
+    return "grid:" + grid_kernel_of(grid);
   }
 
   void allocate(int N) {
@@ -241,6 +490,7 @@ struct EquSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(stage, hX, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
     FPIE_CUDA(cudaMemcpyAsync(stage + (size_t)N * 3, hB, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
     pack_and_check(stage, stage + (size_t)N * 3);
+    choose_mode(hA);
     FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 
@@ -249,6 +499,7 @@ struct EquSolverImpl : Solver {
     allocate(N);
     FPIE_CUDA(cudaMemcpyAsync(A, dA, (size_t)N * 16, cudaMemcpyDeviceToDevice, stream));
     pack_and_check(dX, dB);
+    choose_mode(nullptr);
   }
 
   int* d_rows = nullptr;  // target coordinates of unknowns 1..N-1 (GPU reset)
@@ -319,6 +570,15 @@ struct EquSolverImpl : Solver {
                      t_row + x0, t_col + y0, mode, E.np, A, x[0], x[1], b, d_rows, d_cols, stream);
     post_launch(this);
     ready = true;
+    use_grid = false;
+    lay_N = 0;  // d_pos is rewritten below; the cached placement no longer matches d_occ
+    if (kernel_req != "gather" && N > 1) {  // a mask's system: its pixels are known
+      ensure_pos(N);
+      equ_pos_kernel<<<conv_blocks(N), 256, 0, stream>>>(N, d_rows, d_cols, t_row + x0,
+                                                          t_col + y0, m, d_pos);
+      post_launch(this);
+      enter_grid(n, m);
+    }
     box_out[0] = t_row + x0;
     box_out[1] = t_row + x1;
     box_out[2] = t_col + y0;
@@ -368,6 +628,13 @@ struct EquSolverImpl : Solver {
 
   void run_sweeps(int iters) {
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "step called before reset");
+    if (use_grid) {
+      if (iters > 0) {
+        grid_run(grid, stream, iters);
+        grid_newer = true;
+      }
+      return;
+    }
     while (iters >= kChunk) {
       if (!chunk[cur]) capture_chunk(cur);
       FPIE_CUDA(cudaGraphLaunch(chunk[cur], stream));
@@ -382,6 +649,7 @@ struct EquSolverImpl : Solver {
   }
 
   void finish(uint8_t* img, float* err) {
+    sync_from_grid();
     equ_finish_kernel<<<nparts, 256, 0, stream>>>(E, A, b, x[cur], img ? img : d_img, d_part);
     post_launch(this);
     launch_finalize(d_part, nparts, err ? err : d_err, stream);
@@ -400,6 +668,7 @@ struct EquSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(h_img, d_img, bytes, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaMemcpyAsync(h_err, d_err, 3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
+    check_async();
     std::memcpy(img_out, h_img, bytes);
     std::memcpy(err_out, h_err, 3 * sizeof(float));
   }
@@ -407,12 +676,14 @@ struct EquSolverImpl : Solver {
   void get_state(float* out) {
     FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
+    sync_from_grid();
     AsyncScratch scratch((size_t)E.N * 12, stream);
     float* tmp = reinterpret_cast<float*>(scratch.bytes());
     equ_unpack_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, x[cur], tmp);
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(out, tmp, (size_t)E.N * 12, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
+    check_async();
   }
 };
 
@@ -484,6 +755,44 @@ int fpie_equ_step_device(fpie_solver* s, int iteration, uint8_t* x, float* err) 
     EquSolverImpl* h = equ_of(s);
     h->run_sweeps(iteration);
     if (x || err) h->finish(x, err);
+  });
+}
+
+int fpie_equ_set_kernel(fpie_solver* s, const char* name) {
+  return guarded([&] {
+    FPIE_REQUIRE(name != nullptr, FPIE_ERR_ARG, "null kernel name");
+    equ_of(s)->set_kernel(name);
+  });
+}
+
+int fpie_equ_kernel(fpie_solver* s, char* buf, int len) {
+  return guarded([&] {
+    FPIE_REQUIRE(buf != nullptr && len > 0, FPIE_ERR_ARG, "null or empty buffer");
+    const std::string k = equ_of(s)->kernel_name();
+    std::snprintf(buf, (size_t)len, "%s", k.c_str());
+  });
+}
+
+int fpie_equ_raster_layout(int N, const int32_t* A, int32_t* pos, int* n, int* m) {
+  return guarded([&] {
+    FPIE_REQUIRE(A && pos && n && m, FPIE_ERR_ARG, "null argument");
+    FPIE_REQUIRE(N >= 1, FPIE_ERR_ARG, "N must be at least 1");
+    std::vector<int> p;
+    int nn = 0, mm = 0;
+    FPIE_REQUIRE(raster_embed(N, A, p, nn, mm), FPIE_ERR_ARG, "not a 4-neighbour raster system");
+    pos[0] = -1;
+    for (int i = 1; i < N; ++i) pos[i] = p[i];
+    *n = nn;
+    *m = mm;
+  });
+}
+
+int fpie_equ_set_spin_limit(fpie_solver* s, long long spins) {
+  return guarded([&] {
+    FPIE_REQUIRE(spins >= 0, FPIE_ERR_ARG, "spin limit must be >= 0");
+    EquSolverImpl* h = equ_of(s);
+    h->spin_limit = spins;
+    if (h->grid) grid_set_spin(h->grid, spins);
   });
 }
 

@@ -57,6 +57,44 @@ __global__ void grid_inputs_unpack_kernel(GridGeom G, const uint8_t* __restrict_
 
 // ---- layout conversion kernels ------------------------------------------------
 
+// An equation system that is a 4-neighbour raster stencil, on the grid:
+// unknown i (1..N-1) at crop pixel pos[i] (row-major, G.m per row) gets its
+// X as state and its B as "grad"; every other pixel stays 0 and unmasked,
+// which is what the system's constant row 0 contributes to a gather.
+// X and B are planar (channel c at c * np).
+__global__ void grid_from_equ_kernel(GridGeom G, int N, const int* __restrict__ pos,
+                                     const float* __restrict__ xe, const float* __restrict__ be,
+                                     long long np, uint8_t* __restrict__ mask,
+                                     float* __restrict__ x0, float* __restrict__ x1,
+                                     float* __restrict__ g) {
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int p = pos[i];
+    const long long q = G.at(p / G.m, p % G.m);
+    mask[q] = 1;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float v = xe[c * np + i];
+      x0[c * G.plane + q] = v;
+      x1[c * G.plane + q] = v;
+      g[c * G.plane + q] = be[c * np + i];
+    }
+  }
+}
+
+// The unknowns' state back into planar X (row 0 untouched).
+__global__ void grid_to_equ_kernel(GridGeom G, int N, const int* __restrict__ pos,
+                                   const float* __restrict__ x, float* __restrict__ xe,
+                                   long long np) {
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int p = pos[i];
+    const long long q = G.at(p / G.m, p % G.m);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xe[c * np + i] = x[c * G.plane + q];
+  }
+}
+
 __global__ void grid_pack_kernel(GridGeom G, const int32_t* __restrict__ mk,
                                  const float* __restrict__ t,
                                  const float* __restrict__ gr,
@@ -425,6 +463,33 @@ struct GridSolverImpl : Solver {
     pack(sm, st, sg);
     // The caller may reuse its arrays as soon as reset returns.
     FPIE_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // Loads an equation system that is a 4-neighbour raster stencil (see
+  // grid_from_equ_kernel); the sweeps are then bit-identical to the
+  // system's gather sweeps.
+  void reset_from_equ(int n, int m, int N, const int* pos, const float* xe, const float* be,
+                      long long np) {
+    allocate(n, m);
+    N_user = n * m;
+    const size_t pb = (size_t)G.plane * 3 * sizeof(float);
+    FPIE_CUDA(cudaMemsetAsync(x[0], 0, pb, stream));
+    FPIE_CUDA(cudaMemsetAsync(x[1], 0, pb, stream));
+    FPIE_CUDA(cudaMemsetAsync(g, 0, pb, stream));
+    FPIE_CUDA(cudaMemsetAsync(mask, 0, (size_t)G.plane, stream));
+    if (N > 1) {
+      grid_from_equ_kernel<<<conv_blocks(N), 256, 0, stream>>>(G, N, pos, xe, be, np, mask, x[0],
+                                                               x[1], g);
+      post_launch(this);
+    }
+    ready = true;
+  }
+
+  void to_equ(int N, const int* pos, float* xe, long long np) {
+    FPIE_REQUIRE(ready, FPIE_ERR_STATE, "no state before reset");
+    if (N <= 1) return;
+    grid_to_equ_kernel<<<conv_blocks(N), 256, 0, stream>>>(G, N, pos, x[cur], xe, np);
+    post_launch(this);
   }
 
   void reset_device(int n, int m, const int32_t* dm, const float* dt,
@@ -1179,4 +1244,29 @@ namespace fpie {
 void grid_sweeps(Solver* s, int iters) { static_cast<GridSolverImpl*>(s)->run_sweeps(iters); }
 void grid_get_state(Solver* s, float* out) { static_cast<GridSolverImpl*>(s)->get_state(out); }
 void grid_set_precision(Solver* s, int p) { static_cast<GridSolverImpl*>(s)->set_precision(p); }
+
+// Used by the equation solver to run raster-stencil systems on a grid; each
+// call enqueues on stream `st`.
+void grid_reset_from_equ(Solver* s, cudaStream_t st, int n, int m, int N, const int* pos,
+                         const float* xe, const float* be, long long np) {
+  s->stream = st;
+  static_cast<GridSolverImpl*>(s)->reset_from_equ(n, m, N, pos, xe, be, np);
+}
+void grid_to_equ(Solver* s, cudaStream_t st, int N, const int* pos, float* xe, long long np) {
+  s->stream = st;
+  static_cast<GridSolverImpl*>(s)->to_equ(N, pos, xe, np);
+}
+void grid_run(Solver* s, cudaStream_t st, int iters) {
+  s->stream = st;
+  static_cast<GridSolverImpl*>(s)->run_sweeps(iters);
+}
+void grid_pin_kernel(Solver* s, const std::string& name) {
+  static_cast<GridSolverImpl*>(s)->set_kernel(name);
+}
+std::string grid_kernel_of(Solver* s) { return static_cast<GridSolverImpl*>(s)->kernel_name(); }
+void grid_set_spin(Solver* s, long long spins) {
+  GridSolverImpl* h = static_cast<GridSolverImpl*>(s);
+  if (spins != h->r_spin_limit) h->drop_graphs();
+  h->r_spin_limit = spins;
+}
 }  // namespace fpie

@@ -159,6 +159,32 @@ int fpie_equ_get_index(fpie_solver* s, int32_t* rows, int32_t* cols);
  * float32[N][3]. */
 int fpie_equ_get_inputs(fpie_solver* s, int32_t* A, float* B);
 
+/* How the EquSolver sweeps (reference: the equation sweep of
+ * fpie/core/cuda/equ.cu:76-96 and fpie/np_solver.py:33-41).  "auto"
+ * (default): a system that is a 4-neighbour raster stencil -- the ones
+ * EquProcessor builds from a mask (fpie/process.py:253-265), row 0 constant
+ * and zero -- is placed on a grid and swept by the grid kernels (temporally
+ * blocked, autotuned; same operations in the same order, so bit-identical
+ * results), any other system by the gather kernel.  "gather": always the
+ * gather kernel.  A grid kernel name (see fpie_grid_set_kernel): grid
+ * placement with that kernel, FPIE_ERR_ARG at reset if the system is not a
+ * raster stencil.  Applies from the next reset. */
+int fpie_equ_set_kernel(fpie_solver* s, const char* name);
+
+/* Writes "gather" or "grid:<grid kernel>" (NUL-terminated) into buf. */
+int fpie_equ_kernel(fpie_solver* s, char* buf, int len);
+
+/* Spin limit of the grid kernels' bounded waits in grid placement (see
+ * fpie_grid_set_spin_limit). */
+int fpie_equ_set_spin_limit(fpie_solver* s, long long spins);
+
+/* Host-only: whether A (int32[N][4]: up, down, left, right; 0 = the
+ * constant row 0) is a 4-neighbour raster stencil, and if so a placement:
+ * pos int32[N] (pos[0] = -1; pos[i] = row * m + col of unknown i in an n x m
+ * crop with a 1-pixel frame, connected components one below the other, a
+ * row apart).  FPIE_OK if it is, FPIE_ERR_ARG if not.  No GPU needed. */
+int fpie_equ_raster_layout(int N, const int32_t* A, int32_t* pos, int* n, int* m);
+
 /* Copies the grid inputs the solver holds (mask int32[n][m], grad
  * float32[n][m][3]) to host memory. */
 int fpie_grid_get_inputs(fpie_solver* s, int32_t* mask_out, float* grad_out);

@@ -92,3 +92,98 @@ def test_continuation(backend):
     b.step(70)
     np.testing.assert_array_equal(a.state(), b.state())
     np.testing.assert_array_equal(a.state(), d["equ_state_70"])
+
+
+def _two_disks_system():
+    n0, m0 = 300, 420
+    mask = np.zeros((n0, m0), np.uint8)
+    yy, xx = np.mgrid[:n0, :m0]
+    mask[(yy - 90) ** 2 + (xx - 100) ** 2 < 70 ** 2] = 255
+    mask[(yy - 200) ** 2 + (xx - 300) ** 2 < 90 ** 2] = 255
+    mask[250:260, 20:60] = 255
+    from fpie_gb300 import workloads
+    from oracle import prep
+
+    src = workloads.smooth_image(8, n0, m0, 8)
+    tgt = workloads.smooth_image(9, n0, m0, 8)
+    return prep.equ_inputs(src, mask, tgt, (0, 0), (0, 0), "max")
+
+
+def _same_as_gather(backend, N, A, X, B):
+    """A raster system swept by the grid kernels ("auto") and by the gather
+    kernel: identical states, images and err at every checkpoint."""
+    g = backend.EquSolver(256)
+    g.reset(N, A, X, B)
+    assert g.kernel.startswith("grid:")
+    q = backend.EquSolver(256)
+    q.set_kernel("gather")
+    q.reset(N, A, X, B)
+    assert q.kernel == "gather"
+    for k in (1, 16, 33, 200):
+        xg, eg = g.step(k)
+        xq, eq = q.step(k)
+        np.testing.assert_array_equal(xg, xq)
+        np.testing.assert_array_equal(eg, eq)
+        np.testing.assert_array_equal(g.state(), q.state())
+
+
+def test_grid_placement_equals_gather_golden(backend, golden):
+    _, d = golden
+    _same_as_gather(backend, int(d["equ_N"]), d["equ_A"], d["equ_X"], d["equ_B"])
+
+
+def test_grid_placement_equals_gather_components(backend):
+    d = _two_disks_system()
+    _same_as_gather(backend, d["N"], d["A"], d["X"], d["B"])
+
+
+@pytest.mark.parametrize("kernel", ["p16w8k16", "p16w8k16d", "sweep1"])
+def test_grid_placement_pinned_kernels(backend, kernel):
+    d = _two_disks_system()
+    s = backend.EquSolver(256)
+    s.set_kernel(kernel)
+    s.reset(d["N"], d["A"], d["X"], d["B"])
+    assert s.kernel == "grid:" + kernel
+    s.step(150)
+    o = cjacobi.CEqu(d["A"], d["X"], d["B"])
+    o.sweep(150)
+    np.testing.assert_array_equal(s.state(), o.X)
+
+
+def test_grid_placement_refuses_non_raster(backend):
+    from fpie_gb300 import _abi
+
+    rng = np.random.default_rng(3)
+    N = 64
+    A = rng.integers(0, N, (N, 4)).astype(np.int32)
+    A[0] = 0
+    X = rng.uniform(0, 255, (N, 3)).astype(np.float32)
+    X[0] = 0
+    B = rng.uniform(-20, 20, (N, 3)).astype(np.float32)
+    B[0] = 0
+    s = backend.EquSolver(256)
+    s.reset(N, A, X, B)                 # auto: the gather kernel
+    assert s.kernel == "gather"
+    p = backend.EquSolver(256)
+    p.set_kernel("p16w8k16")
+    with pytest.raises(_abi.FpieArgumentError):
+        p.reset(N, A, X, B)
+
+
+def test_grid_placement_from_images(backend):
+    """The GPU-side reset places the mask's unknowns directly (no search)."""
+    from fpie_gb300 import workloads
+
+    pb = workloads.circle256()
+    s = backend.EquSolver(256)
+    N, box, idx = s.reset_images(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, pb.gradient)
+    assert s.kernel.startswith("grid:")
+    A, B = s.inputs()
+    X0 = s.state()
+    q = backend.EquSolver(256)
+    q.set_kernel("gather")
+    q.reset(N, A, X0, B)
+    xs, es = s.step(300)
+    xq, eq = q.step(300)
+    np.testing.assert_array_equal(xs, xq)
+    np.testing.assert_array_equal(s.state(), q.state())
