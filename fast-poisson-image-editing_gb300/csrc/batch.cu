@@ -142,6 +142,7 @@ struct BQueue {
   const int* act;          // act[z] = jobs (sorted prefix) still active at level z
   const int2* tiles;       // (tile index, flag) per job, concatenated
   int nlevels;
+  int njobs;
   unsigned long long* next;
   int* done;
   int* error;
@@ -158,28 +159,67 @@ __device__ __forceinline__ int upper_bound_idx(const T* a, int n, T v) {
   return lo;
 }
 
+// Item bodies, out of line: inlined into the work loop, the compiler's
+// register assignment needs several times the register moves per sweep of
+// the same code in a launch-per-tile kernel (measured with instruction
+// counters on the grid kernels).
+template <int R, int W, int K, bool FULL, typename TS>
+__device__ __noinline__ void batch_sweep_item(const GridGeom& G, const uint8_t* mask,
+                                              const float* gc, const TS* xc, TS* oc,
+                                              long long base, int ks, int lane, int w,
+                                              float4 (&edge)[2][2][W][32]) {
+  tbp_body<R, W, K, FULL, TS, false, true>(G, mask, gc, xc, oc, base, ks, lane, w, edge);
+}
+
+template <int R, int W, int K, bool FULL, typename TS, bool HASE>
+__device__ __noinline__ void batch_fold_item(const GridGeom& G, const uint8_t* mask,
+                                             const float* gc, const float* xin, const TS* elast,
+                                             float* xout, float* rout, TS* eout, long long base,
+                                             int ks, int lane, int w,
+                                             float4 (&edge)[2][2][W][32]) {
+  tbp_fold_body<R, W, K, FULL, TS, HASE, true>(G, mask, gc, xin, elast, xout, rout, eout, base,
+                                               ks, lane, w, edge);
+}
+
 template <int R, int W, int K, typename TS>
 __global__ void __launch_bounds__(W * 32)
 batch_persistent_kernel(BQueue Q) {
   constexpr bool MIXED = !std::is_same<TS, float>::value;
   constexpr int TH = W * R - 2 * K;
   constexpr int TW = 128 - 2 * K;
+  // The queue tables, in shared memory when they fit: decoding an item is
+  // two binary searches, which through global memory would be ~20 dependent
+  // L2 round trips on every item's critical path.
+  constexpr int kSL = 640, kSJ = 320;
   __shared__ float4 edge[2][2][W][32];
+  __shared__ long long s_lo[kSL + 1], s_ct[kSJ + 1];
+  __shared__ int s_act[kSL], s_order[kSJ];
   __shared__ long long s_idx;
   __shared__ int s_stop;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool fits = Q.nlevels <= kSL && Q.njobs <= kSJ;
+  if (fits) {
+    for (int k = threadIdx.x; k <= Q.nlevels; k += blockDim.x) s_lo[k] = Q.lo[k];
+    for (int k = threadIdx.x; k < Q.nlevels; k += blockDim.x) s_act[k] = Q.act[k];
+    for (int k = threadIdx.x; k <= Q.njobs; k += blockDim.x) s_ct[k] = Q.ct[k];
+    for (int k = threadIdx.x; k < Q.njobs; k += blockDim.x) s_order[k] = Q.order[k];
+  }
+  const long long* lo = fits ? s_lo : Q.lo;
+  const long long* ct = fits ? s_ct : Q.ct;
+  const int* act = fits ? s_act : Q.act;
+  const int* order = fits ? s_order : Q.order;
   const long long total = Q.lo[Q.nlevels];
+  if (threadIdx.x == 0) s_idx = (long long)atomicAdd(Q.next, 1ULL);
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) s_idx = (long long)atomicAdd(Q.next, 1ULL);
-    __syncthreads();
     const long long idx = s_idx;
     if (idx >= total) break;
-    const int z = upper_bound_idx(Q.lo, Q.nlevels + 1, idx) - 1;
-    const long long i = idx - Q.lo[z];
-    const int js = upper_bound_idx(Q.ct, Q.act[z] + 1, i) - 1;
-    const int j = Q.order[js];
+    const int z = upper_bound_idx(lo, Q.nlevels + 1, idx) - 1;
+    const long long i = idx - lo[z];
+    const int js = upper_bound_idx(ct, act[z] + 1, i) - 1;
+    const int j = order[js];
     const BJobDev& J = Q.jobs[j];
-    const int tc = (int)(i - Q.ct[js]);
+    const int tc = (int)(i - ct[js]);
     const int ti = tc / 3, c = tc - 3 * ti;
     if (threadIdx.x == 0) {
       const int need = J.ntiles * 3 * z;
@@ -210,9 +250,9 @@ batch_persistent_kernel(BQueue Q) {
       float* oc = J.x[pin ^ 1] + co;
       const int ks = min(K, J.sweeps - z * K);
       if (tf.y == 2)
-        tbp_body<R, W, K, true, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+        batch_sweep_item<R, W, K, true, float>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
       else
-        tbp_body<R, W, K, false, float, false, true>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
+        batch_sweep_item<R, W, K, false, float>(J.G, J.mask, gc, xc, oc, base, ks, lane, w, edge);
     } else {
       const MixedLevel L = mixed_level(z, J.sweeps, K);
       TS* e0 = static_cast<TS*>(J.e[0]);
@@ -222,17 +262,17 @@ batch_persistent_kernel(BQueue Q) {
         const int xp = (J.parity + (L.cycle > 0 ? L.cycle - 1 : 0)) & 1;
         if (L.cycle > 0) {  // full previous cycles end in e[1]
           if (tf.y == 2)
-            tbp_fold_body<R, W, K, true, TS, true, true>(J.G, J.mask, gc, J.x[xp] + co, e1 + co,
+            batch_fold_item<R, W, K, true, TS, true>(J.G, J.mask, gc, J.x[xp] + co, e1 + co,
                 J.x[xp ^ 1] + co, J.r + co, e0 + co, base, L.k, lane, w, edge);
           else
-            tbp_fold_body<R, W, K, false, TS, true, true>(J.G, J.mask, gc, J.x[xp] + co, e1 + co,
+            batch_fold_item<R, W, K, false, TS, true>(J.G, J.mask, gc, J.x[xp] + co, e1 + co,
                 J.x[xp ^ 1] + co, J.r + co, e0 + co, base, L.k, lane, w, edge);
         } else {
           if (tf.y == 2)
-            tbp_fold_body<R, W, K, true, TS, false, true>(J.G, J.mask, gc, J.x[xp] + co, nullptr,
+            batch_fold_item<R, W, K, true, TS, false>(J.G, J.mask, gc, J.x[xp] + co, nullptr,
                 nullptr, J.r + co, e0 + co, base, L.k, lane, w, edge);
           else
-            tbp_fold_body<R, W, K, false, TS, false, true>(J.G, J.mask, gc, J.x[xp] + co, nullptr,
+            batch_fold_item<R, W, K, false, TS, false>(J.G, J.mask, gc, J.x[xp] + co, nullptr,
                 nullptr, J.r + co, e0 + co, base, L.k, lane, w, edge);
         }
       } else if (L.type == 1) {
@@ -240,9 +280,9 @@ batch_persistent_kernel(BQueue Q) {
         TS* eout = (L.pos & 1) ? e1 : e0;
         const float* rc = J.r + co;
         if (tf.y == 2)
-          tbp_body<R, W, K, true, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
+          batch_sweep_item<R, W, K, true, TS>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
         else
-          tbp_body<R, W, K, false, TS, false, true>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
+          batch_sweep_item<R, W, K, false, TS>(J.G, J.mask, rc, ein + co, eout + co, base, L.k, lane, w, edge);
       } else {
         const int xp = (J.parity + L.cycle - 1) & 1;
         const TS* elast = (((L.nlast - 1) & 1) ? e1 : e0) + co;
@@ -250,9 +290,19 @@ batch_persistent_kernel(BQueue Q) {
                         ty * TH, tx * TW, TH, TW);
       }
     }
+    // The next item is taken now, so that the atomic's round trip overlaps
+    // the fence and barrier below.  (A CTA then holds two items; the lowest
+    // unfinished item is still always one being worked on, whose waits are
+    // for lower items only: no deadlock.)
+    unsigned long long nxt = 0;
+    if (threadIdx.x == 0) nxt = atomicAdd(Q.next, 1ULL);
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(Q.done + j, 1);
+    if (threadIdx.x == 0) {
+      atomicAdd(Q.done + j, 1);
+      s_idx = (long long)nxt;
+    }
+    __syncthreads();
   }
 }
 
@@ -566,6 +616,7 @@ struct Batch {
       q.next = reinterpret_cast<unsigned long long*>(dev + off);
       q.error = reinterpret_cast<int*>(dev + off + 8);
       q.nlevels = nlevels;
+      q.njobs = nj;
       q.spin_limit = spin_limit;
       FPIE_CUDA(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, stream));
       int occ = 0;
