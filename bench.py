@@ -76,6 +76,26 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def job_time_max(ms: float, world: int, device=None) -> float:
+    """The whole job's time: the max over ranks of each rank's timed
+    milliseconds (with N > 1 every rank runs an independent replica; the
+    path has no exchange step).  `device` None = a CPU tensor (gloo)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(units_per_step: float, steps: int, world: int, ms: float) -> float:
+    """Units all ranks processed (each rank the same replica work) per second
+    of the slowest rank's time."""
+    return units_per_step * steps * world / (ms / 1e3)
+
+
 def host_threads() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -322,11 +342,8 @@ def run_gb300(args):
 
     step_ms = sum(a for a, _ in times)
     sweep_ms = sum(b for _, b in times)
-    if world > 1:
-        tt = torch.tensor([step_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(tt.item())
-    value = unknowns * sweeps * args.steps * world / (step_ms / 1e3)
+    step_ms = job_time_max(step_ms, world, dev)
+    value = whole_job_value(unknowns * sweeps, args.steps, world, step_ms)
 
     # Parity spot check of the timed path's output against a fresh solve.
     check = backend.GridSolver(8, 8)
