@@ -174,13 +174,18 @@ struct GridSolverImpl : Solver {
   int tma_list_cap = 0;
   int tma_grid = 0;          // persistent CTAs for the current tiling
 
-  // ---- dependency-flow kernel (variant index kFlow) ---------------------------
-  // Shares the active-tile list and the wait-error flag with the TMA kernel.
+  // ---- dependency-flow kernel (FP32: variant kFlow; mixed: mvariant kFlow) ---
+  // Its tables depend only on the geometry and the mask; it shares the
+  // wait-error flag with the TMA kernel.
   static constexpr int kFlow = -4;
-  int* flow_inv = nullptr;   // tile -> active-list index
-  void* flow_rec = nullptr;  // per active tile: index, flag, neighbourhood
-  int* flow_done = nullptr;  // levels finished per (active tile, channel)
-  int flow_cap = 0;          // tiles the two arrays hold
+  uint8_t* ft_flags = nullptr;  // tile flags for the flow tiling
+  int* ft_list = nullptr;       // active-tile list (count + indices)
+  int* flow_inv = nullptr;      // tile -> active-list index
+  void* flow_rec = nullptr;     // per active tile: index, flag, neighbourhood
+  int* flow_done = nullptr;     // levels finished per (active tile, channel)
+  int flow_cap = 0;             // tiles the arrays hold
+  int ft_tiles_x = 0, ft_tiles = 0;
+  bool ft_ok = false;
   int flow_grid = 0;
 
   // Reads and clears the TMA kernel's time-out flag; call after the stream
@@ -274,13 +279,27 @@ struct GridSolverImpl : Solver {
   // All `iters` sweeps in one launch of the dependency-flow kernel.  A wait
   // that timed out is reported at the next host synchronisation.
   void run_flow(int iters) {
-    ensure_flags();
-    FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)tiles * 3 * sizeof(int), stream));
-    launch_flow(G, mask, g, x[0], x[1], cur, tma_list, flow_rec, flow_done, tiles_x, tiles, iters,
-                d_tma_err, r_spin_limit, flow_grid, stream);
+    ensure_flow_tables();
+    FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
+    launch_flow(G, mask, g, x[0], x[1], cur, ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles,
+                iters, d_tma_err, r_spin_limit, flow_grid, stream);
     post_launch(this);
     const int levels = (iters + flow_depth() - 1) / flow_depth();
     if (levels & 1) cur ^= 1;
+  }
+
+  // The mixed forms as one flow launch (cycles of 64 sweeps and the final
+  // fold, like run_mixed's launch sequence with a 16-sweep kernel).
+  void run_flow_mixed(int iters) {
+    ensure_mixed();
+    ensure_flow_tables();
+    FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
+    launch_flow_mixed(G, mask, g, x[0], x[1], cur, precision == FPIE_MIXED_BF16, e[0], e[1], r,
+                      ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles, iters, d_tma_err,
+                      r_spin_limit, flow_grid, stream);
+    post_launch(this);
+    if (flow_mixed_flips(iters) & 1) cur ^= 1;
+    e_pending = false;
   }
 
   // All `iters` sweeps in one cooperative launch.
@@ -382,10 +401,15 @@ struct GridSolverImpl : Solver {
     cudaFree(flow_inv);
     cudaFree(flow_done);
     cudaFree(flow_rec);
+    cudaFree(ft_flags);
+    cudaFree(ft_list);
     flow_inv = nullptr;
     flow_done = nullptr;
     flow_rec = nullptr;
+    ft_flags = nullptr;
+    ft_list = nullptr;
     flow_cap = 0;
+    ft_ok = false;
     if (h_tma_err) cudaFreeHost(h_tma_err);
     d_tma_err = nullptr;
     h_tma_err = nullptr;
@@ -413,6 +437,7 @@ struct GridSolverImpl : Solver {
       ready = false;
       flags_ok = false;  // the new mask may activate other tiles
       mflags_ok = false;
+      ft_ok = false;
       r_ok = false;
       return;
     }
@@ -556,6 +581,7 @@ struct GridSolverImpl : Solver {
     ready = true;
     flags_ok = false;
     mflags_ok = false;
+    ft_ok = false;
     r_ok = false;
     box_out[0] = t_row + x0;
     box_out[1] = t_row + x1;
@@ -603,13 +629,17 @@ struct GridSolverImpl : Solver {
   }
 
   void ensure_flags() {
+    if (variant == kFlow) {
+      ensure_flow_tables();
+      return;
+    }
     // sweep1 / resident: no flags
-    if (flags_ok || (variant < 0 && variant != kTma && variant != kFlow)) return;
-    const bool tma = variant == kTma, flow = variant == kFlow;
-    const bool listed = tma || flow;  // kernels that take the active-tile list
-    const int th = tma ? tma_tile_h() : flow ? flow_tile_h() : tb_variants()[variant].tile_h;
-    const int tw = tma ? tma_tile_w() : flow ? flow_tile_w() : tb_variants()[variant].tile_w;
-    const int kd = tma ? tma_depth() : flow ? flow_depth() : tb_variants()[variant].depth;
+    if (flags_ok || (variant < 0 && variant != kTma)) return;
+    const bool tma = variant == kTma;
+    const bool listed = tma;  // kernels that take the active-tile list
+    const int th = tma ? tma_tile_h() : tb_variants()[variant].tile_h;
+    const int tw = tma ? tma_tile_w() : tb_variants()[variant].tile_w;
+    const int kd = tma ? tma_depth() : tb_variants()[variant].depth;
     tiles_x = (G.m + tw - 1) / tw;
     tiles = tiles_x * ((G.n + th - 1) / th);
     if (tiles > flags_cap) {
@@ -619,29 +649,9 @@ struct GridSolverImpl : Solver {
       flags_cap = tiles;
     }
     if (listed) {
-      if (tma) {
-        prepare_tma();
-        tma_grid = tma_ctas(tiles * 3);
-      } else {
-        flow_grid = flow_ctas();
-        if (tiles > flow_cap) {
-          cudaFree(flow_inv);
-          cudaFree(flow_done);
-          cudaFree(flow_rec);
-          flow_inv = flow_done = nullptr;
-          flow_rec = nullptr;
-          FPIE_CUDA(cudaMalloc(&flow_inv, (size_t)tiles * sizeof(int)));
-          FPIE_CUDA(cudaMalloc(&flow_done, (size_t)tiles * 3 * sizeof(int)));
-          FPIE_CUDA(cudaMalloc(&flow_rec, (size_t)tiles * flow_rec_bytes()));
-          flow_cap = tiles;
-        }
-      }
-      if (!d_tma_err) {
-        FPIE_CUDA(cudaMalloc(&d_tma_err, sizeof(int)));
-        FPIE_CUDA(cudaMallocHost(&h_tma_err, sizeof(int)));
-        *h_tma_err = 0;
-        FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
-      }
+      prepare_tma();
+      tma_grid = tma_ctas(tiles * 3);
+      ensure_wait_flag();
       if (tiles + 1 > tma_list_cap) {
         cudaFree(tma_list);
         tma_list = nullptr;
@@ -657,11 +667,48 @@ struct GridSolverImpl : Solver {
       launch_tma_list(flags, tiles, tma_list, stream);
       post_launch(this);
     }
-    if (flow) {
-      launch_flow_tables(tma_list, flags, tiles_x, tiles, flow_inv, flow_rec, stream);
-      post_launch(this);
-    }
     flags_ok = true;
+  }
+
+  void ensure_wait_flag() {
+    if (d_tma_err) return;
+    FPIE_CUDA(cudaMalloc(&d_tma_err, sizeof(int)));
+    FPIE_CUDA(cudaMallocHost(&h_tma_err, sizeof(int)));
+    *h_tma_err = 0;
+    FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
+  }
+
+  // Flags, active-tile list, records and counters of the flow tiling.
+  void ensure_flow_tables() {
+    if (ft_ok) return;
+    const int th = flow_tile_h(), tw = flow_tile_w(), kd = flow_depth();
+    ft_tiles_x = (G.m + tw - 1) / tw;
+    ft_tiles = ft_tiles_x * ((G.n + th - 1) / th);
+    if (ft_tiles > flow_cap) {
+      cudaFree(flow_inv);
+      cudaFree(flow_done);
+      cudaFree(flow_rec);
+      cudaFree(ft_flags);
+      cudaFree(ft_list);
+      flow_inv = flow_done = ft_list = nullptr;
+      flow_rec = nullptr;
+      ft_flags = nullptr;
+      FPIE_CUDA(cudaMalloc(&ft_flags, (size_t)ft_tiles));
+      FPIE_CUDA(cudaMalloc(&ft_list, (size_t)(ft_tiles + 1) * sizeof(int)));
+      FPIE_CUDA(cudaMalloc(&flow_inv, (size_t)ft_tiles * sizeof(int)));
+      FPIE_CUDA(cudaMalloc(&flow_done, (size_t)ft_tiles * 3 * sizeof(int)));
+      FPIE_CUDA(cudaMalloc(&flow_rec, (size_t)ft_tiles * flow_rec_bytes()));
+      flow_cap = ft_tiles;
+    }
+    flow_grid = flow_ctas();
+    ensure_wait_flag();
+    launch_tile_flags(G, mask, th, tw, kd, ft_tiles_x, ft_tiles, ft_flags, stream);
+    post_launch(this);
+    launch_tma_list(ft_flags, ft_tiles, ft_list, stream);
+    post_launch(this);
+    launch_flow_tables(ft_list, ft_flags, ft_tiles_x, ft_tiles, flow_inv, flow_rec, stream);
+    post_launch(this);
+    ft_ok = true;
   }
 
   void select_variant(int v) {
@@ -859,7 +906,7 @@ struct GridSolverImpl : Solver {
       e_prec = precision;
       drop_graphs();
     }
-    if (!mflags_ok) {
+    if (!mflags_ok && mvariant >= 0) {
       const MixedVariant& v = mixed_variants()[mvariant];
       mtiles_x = (G.m + v.tile_w - 1) / v.tile_w;
       mtiles = mtiles_x * ((G.n + v.tile_h - 1) / v.tile_h);
@@ -1000,6 +1047,30 @@ struct GridSolverImpl : Solver {
         }
       }
     }
+    // The flow kernel: whole launches of 4 cycles, per 64 sweeps.
+    if (iters - used >= (kTuneReps + 1) * 4 * kRefine) {
+      if (e_pending) {  // fold the candidates' pending correction first
+        mixed_flush(stream);
+        post_launch(this);
+      }
+      select_mixed(kFlow);
+      run_flow_mixed(4 * kRefine);
+      used += 4 * kRefine;
+      for (int rep = 0; rep < kTuneReps; ++rep) {
+        FPIE_CUDA(cudaEventRecord(e0, stream));
+        run_flow_mixed(4 * kRefine);
+        FPIE_CUDA(cudaEventRecord(e1, stream));
+        FPIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        used += 4 * kRefine;
+        if (ms / 4 < best_ms) {
+          best_ms = ms / 4;
+          best = kFlow;
+        }
+      }
+      check_tma();
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     select_mixed(best);
@@ -1018,6 +1089,10 @@ struct GridSolverImpl : Solver {
     ensure_mixed();
     e_pending = false;  // a step starts from a folded x
     if (!mtuned && !pinned) iters -= autotune_mixed(iters);
+    if (mvariant == kFlow) {
+      if (iters > 0) run_flow_mixed(iters);
+      return;
+    }
     ensure_mixed();
     while (iters >= kRefine) {
       run_cycle_graph();
@@ -1072,10 +1147,11 @@ struct GridSolverImpl : Solver {
       return;
     }
     if (precision != FPIE_FP32) {
-      int v = -1;
+      int v = -100;
+      if (name == "p16w8k16d") v = kFlow;
       for (size_t k = 0; k < mixed_variants().size(); ++k)
         if (name == mixed_variants()[k].name) v = (int)k;
-      FPIE_REQUIRE(v >= 0, FPIE_ERR_ARG, "unknown mixed-precision grid kernel '" + name + "'");
+      FPIE_REQUIRE(v != -100, FPIE_ERR_ARG, "unknown mixed-precision grid kernel '" + name + "'");
       select_mixed(v);
       pinned = true;
       return;
@@ -1093,7 +1169,8 @@ struct GridSolverImpl : Solver {
   }
 
   std::string kernel_name() const {
-    if (precision != FPIE_FP32) return std::string(mixed_variants()[mvariant].name);
+    if (precision != FPIE_FP32)
+      return mvariant == kFlow ? std::string("p16w8k16d") : std::string(mixed_variants()[mvariant].name);
     if (variant == kResident) return std::string("res16w8k4");
     if (variant == kTma) return std::string("p16w8k16t");
     if (variant == kFlow) return std::string("p16w8k16d");

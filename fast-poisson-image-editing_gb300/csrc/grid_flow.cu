@@ -29,8 +29,11 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include <type_traits>
+
 #include "grid_flow.cuh"
 #include "grid_tbp.cuh"
+#include "mixed_levels.cuh"
 
 namespace fpie {
 
@@ -53,6 +56,8 @@ struct FlowArgs {
   const uint8_t* mask;
   const float* g;
   float* x[2];
+  void* e[2];            // mixed forms: the correction planes (FP16 / BF16)
+  float* r;              // mixed forms: the FP32 residual planes
   const int* list;       // active tiles in tile order; list[-1] = their count
   const FlowRec* rec;    // per active tile
   int* done;             // per (active tile, channel): levels finished
@@ -121,12 +126,54 @@ __device__ __noinline__ void flow_item(const FlowArgs& A, int tile, int c, int z
 // the current item's sweeps so that their latency overlaps the release
 // fence and barrier; the other threads get tile and flag through shared
 // memory.
+// One item of the mixed forms at level z: the batched kernel's level
+// schedule (mixed_level: fold + first inner sweeps, inner sweeps on the
+// correction, final fold), on one (tile, channel).  Out of line like
+// flow_item.
+template <bool FULL, typename TS>
+__device__ __noinline__ void flow_mixed_item(const FlowArgs& A, int tile, int c, int z,
+                                             float4 (&edge)[2][2][kW][32], int lane, int w) {
+  const GridGeom& G = A.G;
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long co = c * G.plane;
+  const float* gc = A.g + co;
+  TS* e0 = static_cast<TS*>(A.e[0]);
+  TS* e1 = static_cast<TS*>(A.e[1]);
+  const MixedLevel L = mixed_level(z, A.sweeps, kK);
+  if (L.type == 0) {
+    // x parity before this cycle's fold: one flip per earlier fold.
+    const int xp = (A.parity + (L.cycle > 0 ? L.cycle - 1 : 0)) & 1;
+    if (L.cycle > 0)  // full previous cycles end in e[1]
+      tbp_fold_body<kR, kW, kK, FULL, TS, true, true>(G, A.mask, gc, A.x[xp] + co, e1 + co,
+                                                      A.x[xp ^ 1] + co, A.r + co, e0 + co, base,
+                                                      L.k, lane, w, edge);
+    else
+      tbp_fold_body<kR, kW, kK, FULL, TS, false, true>(G, A.mask, gc, A.x[xp] + co, nullptr,
+                                                       nullptr, A.r + co, e0 + co, base, L.k,
+                                                       lane, w, edge);
+  } else if (L.type == 1) {
+    const TS* ein = ((L.pos - 1) & 1) ? e1 : e0;
+    TS* eout = (L.pos & 1) ? e1 : e0;
+    tbp_body<kR, kW, kK, FULL, TS, false, true>(G, A.mask, A.r + co, ein + co, eout + co, base,
+                                                L.k, lane, w, edge);
+  } else {
+    const int xp = (A.parity + L.cycle - 1) & 1;
+    const TS* elast = (((L.nlast - 1) & 1) ? e1 : e0) + co;
+    refine_tile<TS>(G, A.mask, gc, A.x[xp] + co, elast, A.x[xp ^ 1] + co, nullptr, ty * kTH,
+                    tx * kTW, kTH, kTW);
+  }
+}
+
+// TS = float: the FP32 sweeps; __half / __nv_bfloat16: the mixed forms.
+template <typename TS>
 __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
+  constexpr bool MIXED = !std::is_same<TS, float>::value;
   __shared__ float4 edge[2][2][kW][32];
   __shared__ int s_stop, s_tile, s_flag;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int per = 3 * A.list[-1];
-  const int levels = (A.sweeps + kK - 1) / kK;
+  const int levels = MIXED ? mixed_levels(A.sweeps, kK) : (A.sweeps + kK - 1) / kK;
   const long long total = (long long)levels * per;
   FlowRec R{};
   int v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -148,10 +195,16 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
     __syncthreads();
     if (s_stop) break;
     const int tile = s_tile;
-    if (s_flag == 2)
+    if (MIXED) {
+      if (s_flag == 2)
+        flow_mixed_item<true, TS>(A, tile, c, z, edge, lane, w);
+      else
+        flow_mixed_item<false, TS>(A, tile, c, z, edge, lane, w);
+    } else if (s_flag == 2) {
       flow_item<true>(A, tile, c, z, edge, lane, w);
-    else
+    } else {
       flow_item<false>(A, tile, c, z, edge, lane, w);
+    }
     const long long next = idx + gridDim.x;
     if (threadIdx.x == 0 && next < total) {
       const int rn = (int)(next % per);
@@ -206,9 +259,15 @@ int flow_ctas() {
   int dev = 0, sms = 0, per_sm = 0;
   FPIE_CUDA(cudaGetDevice(&dev));
   FPIE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_flow_kernel, kW * 32, 0));
-  FPIE_REQUIRE(per_sm >= 1, FPIE_ERR_CUDA, "the flow sweep kernel does not fit on an SM");
-  return sms * per_sm;
+  int m = 1 << 30;
+  const void* ks[3] = {(const void*)grid_flow_kernel<float>, (const void*)grid_flow_kernel<__half>,
+                       (const void*)grid_flow_kernel<__nv_bfloat16>};
+  for (const void* k : ks) {
+    FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kW * 32, 0));
+    m = std::min(m, per_sm);
+  }
+  FPIE_REQUIRE(m >= 1, FPIE_ERR_CUDA, "the flow sweep kernel does not fit on an SM");
+  return sms * m;
 }
 
 void launch_flow_tables(const int* list, const uint8_t* flags, int tiles_x, int tiles, int* inv,
@@ -227,11 +286,29 @@ void launch_flow(const GridGeom& G, const uint8_t* mask, const float* g, float* 
   FPIE_REQUIRE(sweeps >= 1, FPIE_ERR_ARG, "flow sweep kernel: at least one sweep");
   FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
                "flow sweep kernel: bad tiling");
-  FlowArgs a{G, mask, g, {x0, x1}, list + 1, static_cast<const FlowRec*>(rec), done, error,
-             tiles_x, sweeps, parity & 1, spin_limit};
+  FlowArgs a{G, mask, g, {x0, x1}, {nullptr, nullptr}, nullptr, list + 1,
+             static_cast<const FlowRec*>(rec), done, error, tiles_x, sweeps, parity & 1,
+             spin_limit};
   void* args[] = {&a};
-  FPIE_CUDA(cudaLaunchCooperativeKernel((const void*)grid_flow_kernel, dim3(ctas), dim3(kW * 32),
-                                        args, 0, st));
+  FPIE_CUDA(cudaLaunchCooperativeKernel((const void*)grid_flow_kernel<float>, dim3(ctas),
+                                        dim3(kW * 32), args, 0, st));
 }
+
+void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
+                       int parity, bool bf16, void* e0, void* e1, float* r, const int* list,
+                       const void* rec, int* done, int tiles_x, int tiles, int sweeps, int* error,
+                       long long spin_limit, int ctas, cudaStream_t st) {
+  FPIE_REQUIRE(sweeps >= 1, FPIE_ERR_ARG, "flow sweep kernel: at least one sweep");
+  FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
+               "flow sweep kernel: bad tiling");
+  FlowArgs a{G, mask, g, {x0, x1}, {e0, e1}, r, list + 1, static_cast<const FlowRec*>(rec), done,
+             error, tiles_x, sweeps, parity & 1, spin_limit};
+  void* args[] = {&a};
+  const void* k = bf16 ? (const void*)grid_flow_kernel<__nv_bfloat16>
+                       : (const void*)grid_flow_kernel<__half>;
+  FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, 0, st));
+}
+
+int flow_mixed_flips(int sweeps) { return (sweeps + 63) / 64; }
 
 }  // namespace fpie

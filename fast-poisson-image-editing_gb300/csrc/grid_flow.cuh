@@ -31,4 +31,15 @@ void launch_flow(const GridGeom& G, const uint8_t* mask, const float* g, float* 
                  int parity, const int* list, const void* rec, int* done, int tiles_x, int tiles,
                  int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st);
 
+// The mixed forms (FP16 / BF16 correction, FP32 residual every 64 sweeps)
+// as one launch: the level schedule of the batched kernel (mixed_levels),
+// items scheduled like launch_flow.  The folded state ends in buffer
+// (parity + flow_mixed_flips(sweeps)) & 1; e0/e1/r are the solver's
+// correction and residual planes.
+void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
+                       int parity, bool bf16, void* e0, void* e1, float* r, const int* list,
+                       const void* rec, int* done, int tiles_x, int tiles, int sweeps, int* error,
+                       long long spin_limit, int ctas, cudaStream_t st);
+int flow_mixed_flips(int sweeps);
+
 }  // namespace fpie

@@ -74,12 +74,29 @@ def test_every_mixed_kernel(problem, precision):
 
     ref = _solver(problem)
     ref.step(300)
-    for name in ("p16w8k16", "p8w16k16", "p16w8k8"):
+    for name in ("p16w8k16", "p8w16k16", "p16w8k8", "p16w8k16d"):
         s = _solver(problem, precision, name)
         assert s.kernel == name
         s.step(300)  # 4 full cycles and one of 44 sweeps
         d = np.abs(s.state() - ref.state()).max()
         assert d <= (0.25 if precision == "fp16" else 2.0), (name, d)
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+@pytest.mark.parametrize("sweeps", [1, 16, 64, 100, 300])
+def test_mixed_flow_equals_launch_sequence(problem, precision, sweeps):
+    """The mixed forms as one dependency-flow launch perform, per tile, the
+    same operations at the same rounding points as the launch sequence of
+    the 16-sweep packed kernel (fold + 3 inner launches per 64-sweep cycle,
+    final fold): identical states, images and err."""
+    a = _solver(problem, precision, "p16w8k16d")
+    b = _solver(problem, precision, "p16w8k16")
+    for _ in range(2):  # two steps: each starts from a folded state
+        ia, ea = a.step(sweeps)
+        ib, eb = b.step(sweeps)
+        np.testing.assert_array_equal(a.state(), b.state())
+        np.testing.assert_array_equal(ia, ib)
+        np.testing.assert_array_equal(ea, eb)
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
