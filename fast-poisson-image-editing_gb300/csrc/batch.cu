@@ -108,6 +108,10 @@ batch_persistent_kernel(BQueue Q) {
   __shared__ int s_act[kSL], s_order[kSJ];
   __shared__ long long s_idx;
   __shared__ int s_stop;
+  __shared__ int2 s_tf;
+  // The current item's job record, copied by warp 0 (one round trip) so
+  // that the CTA does not chase it field by field through global memory.
+  __shared__ __align__(16) BJobDev s_job;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const bool fits = Q.nlevels <= kSL && Q.njobs <= kSJ;
   if (fits) {
@@ -130,10 +134,18 @@ batch_persistent_kernel(BQueue Q) {
     const long long i = idx - lo[z];
     const int js = upper_bound_idx(ct, act[z] + 1, i) - 1;
     const int j = order[js];
-    const BJobDev& J = Q.jobs[j];
     const int tc = (int)(i - ct[js]);
     const int ti = tc / 3, c = tc - 3 * ti;
+    if (w == 0) {
+      static_assert(sizeof(BJobDev) % 4 == 0, "job record in words");
+      const int* src = reinterpret_cast<const int*>(Q.jobs + j);
+      int* dst = reinterpret_cast<int*>(&s_job);
+      for (int k = lane; k < (int)(sizeof(BJobDev) / 4); k += 32) dst[k] = src[k];
+      __syncwarp();
+    }
+    const BJobDev& J = s_job;
     if (threadIdx.x == 0) {
+      s_tf = Q.tiles[J.tile_off + ti];
       const int need = J.ntiles * 3 * z;
       long long spins = 0;
       int stop = 0;
@@ -151,7 +163,7 @@ batch_persistent_kernel(BQueue Q) {
     }
     __syncthreads();
     if (s_stop) break;
-    const int2 tf = Q.tiles[J.tile_off + ti];
+    const int2 tf = s_tf;
     const int ty = tf.x / J.tiles_x, tx = tf.x - ty * J.tiles_x;
     const long long base = J.G.at(ty * TH - K + w * R, tx * TW - K + 4 * lane);
     const long long co = c * J.G.plane;
@@ -208,9 +220,12 @@ batch_persistent_kernel(BQueue Q) {
     // for lower items only: no deadlock.)
     unsigned long long nxt = 0;
     if (threadIdx.x == 0) nxt = atomicAdd(Q.next, 1ULL);
-    __threadfence();
+    // Release, as a grid-wide barrier does it: the CTA barrier orders every
+    // thread's writes before thread 0's fence, which orders them before the
+    // counter update.
     __syncthreads();
     if (threadIdx.x == 0) {
+      __threadfence();
       atomicAdd(Q.done + j, 1);
       s_idx = (long long)nxt;
     }
