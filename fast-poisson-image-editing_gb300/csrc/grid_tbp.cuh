@@ -189,6 +189,25 @@ template <int R, int W, bool FULL, bool GS>
 __device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (&Gp)[GS ? 1 : R / 2][4],
                                            const uint32_t (&mk)[R], int ksweeps, int lane, int w,
                                            float4 (&edge)[2][2][W][32], const float2* __restrict__ sg) {
+  constexpr int H = R / 2;
+  // A warp whose strip holds no masked pixel (small paste jobs leave most
+  // of a region's strips so) keeps publishing its edge rows and taking part
+  // in the barriers, but skips the updates: its values never change.
+  if (!FULL) {
+    uint32_t any = 0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) any |= mk[i];
+    if (__all_sync(0xffffffffu, any == 0u)) {
+      const float4 top = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+      const float4 bot = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+      for (int s = 0; s < ksweeps; ++s) {
+        edge[s & 1][0][w][lane] = top;
+        edge[s & 1][1][w][lane] = bot;
+        __syncthreads();
+      }
+      return;
+    }
+  }
   int s = 0;
   for (; s + 2 <= ksweeps; s += 2) {
     tbp_sweep<R, W, FULL, GS, true>(P, Gp, mk, 0, lane, w, edge, sg);
