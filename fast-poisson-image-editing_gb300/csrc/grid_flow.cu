@@ -80,6 +80,11 @@ __device__ __forceinline__ void load_counters(const FlowArgs& A, const FlowRec& 
     v[k] = R.nb[k] >= 0 ? *(const volatile int*)(A.done + R.nb[k] + c) : 0x7fffffff;
 }
 
+// Publishes a finished item: a release reduction on its counter.
+__device__ __forceinline__ void release_add(int* counter) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], 1;" : : "l"(counter) : "memory");
+}
+
 __device__ __forceinline__ bool counters_reach(const int (&v)[9], int level) {
   bool ok = true;
 #pragma unroll
@@ -211,14 +216,10 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
       R = load_rec(A.rec + rn / 3);
       load_counters(A, R, rn % 3, v);
     }
-    // Release, as a grid-wide barrier does it: the CTA barrier orders every
-    // thread's writes before thread 0's fence, which orders them before the
-    // counter update.
+    // Release: the CTA barrier orders every thread's writes before thread
+    // 0's release reduction, which makes them visible before the count.
     __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(A.done + 3 * a + c, 1);
-    }
+    if (threadIdx.x == 0) release_add(A.done + 3 * a + c);
   }
 }
 
