@@ -220,13 +220,11 @@ batch_persistent_kernel(BQueue Q) {
     // for lower items only: no deadlock.)
     unsigned long long nxt = 0;
     if (threadIdx.x == 0) nxt = atomicAdd(Q.next, 1ULL);
-    // Release, as a grid-wide barrier does it: the CTA barrier orders every
-    // thread's writes before thread 0's fence, which orders them before the
-    // counter update.
+    // Release: the CTA barrier orders every thread's writes before thread
+    // 0's release reduction, which makes them visible before the count.
     __syncthreads();
     if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(Q.done + j, 1);
+      asm volatile("red.release.gpu.global.add.s32 [%0], 1;" : : "l"(Q.done + j) : "memory");
       s_idx = (long long)nxt;
     }
     __syncthreads();
