@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
     const int a = r / 3, c = r - 3 * a;
     if (threadIdx.x == 0) {
       const bool ok = z == 0 || wait_counters(A, R, c, z, v);
-      __threadfence();  // acquire: the neighbours' writes before our reads
+      // Acquire: the counters read above (relaxed) order the neighbours'
+      // published writes before every read that follows the barrier below.
+      asm volatile("fence.acq_rel.gpu;" ::: "memory");
       s_stop = !ok;
       s_tile = R.tile;
       s_flag = R.flag;
