@@ -18,7 +18,10 @@ Printed JSON line (rank 0):
                 launch duration, against the measured HBM copy bandwidth;
 * ``cpu_baseline`` the oracle's C restatement (OpenMP, all host threads) on a
                 bounded number of sweeps of the same problem;
-* ``equ``       the EquSolver form of the same problem, device-timed.
+* ``equ``       the EquSolver form of the same problem, device-timed;
+* ``mixed_fp16`` the FP16-correction refinement form, device-timed;
+* ``error_vs_fp64`` (with the CPU baseline) how far the 5000-sweep result is
+                from the converged FP64 solution of the same system.
 
 ``--impl reference`` times the CPU implementation of the path instead (the
 C restatement of the reference's Jacobi solvers, all host threads), on a
@@ -220,6 +223,22 @@ def cpu_baseline_grid(mc, t, g, budget_s: float = 10.0):
     return {"value": unknowns * n_sw / dt, "unit": "pixel-updates/s", "cores": th, "kind": "port",
             "sample": f"{n_sw} of {SWEEPS} sweeps of square800 GridSolver (640,000 unknowns) + residual + "
                       f"clip, oracle C restatement (OpenMP), {th} threads, {dt:.2f} s"}
+
+
+def error_vs_fp64(mc, t, g, x) -> dict:
+    """How far a result is from the converged solution: max and mean |x - x64|
+    over masked pixels (intensity units), x64 from the oracle's FP64
+    conjugate gradient (checked against a direct solve in the tests)."""
+    from oracle import fp64
+
+    t0 = time.perf_counter()
+    x64 = fp64.cg_torch(mc, t, g, device="cuda", rtol=1e-12)
+    d = np.abs(x.astype(np.float64) - x64)[np.asarray(mc) != 0]
+    return {"max_abs": float(d.max()), "mean_abs": float(d.mean()), "unit": "intensity (LSB)",
+            "sweeps": SWEEPS, "reference": "FP64 conjugate gradient, rtol 1e-12",
+            "seconds": round(time.perf_counter() - t0, 2),
+            "note": "the benchmark's 5000 Jacobi sweeps are far from converged on an "
+                    "800x800 paste; the precision study runs to <= 0.5 LSB"}
 
 
 def run_reference(args):
@@ -480,6 +499,8 @@ def run_gb300(args):
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_grid(mc, t, g)
+        if sweeps == SWEEPS:
+            line["error_vs_fp64"] = error_vs_fp64(mc, t, g, check.state())
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
