@@ -21,7 +21,10 @@ Printed JSON line (rank 0):
 * ``equ``       the EquSolver form of the same problem, device-timed;
 * ``mixed_fp16`` the FP16-correction refinement form, device-timed;
 * ``error_vs_fp64`` (with the CPU baseline) how far the 5000-sweep result is
-                from the converged FP64 solution of the same system.
+                from the converged FP64 solution of the same system;
+* ``reference_cuda`` (with the CPU baseline) the reference's own CUDA
+                solvers on the same GPU: step time at 5000 sweeps, and the
+                GB300 backend's sweeps and time to the same residual.
 
 ``--impl reference`` times the CPU implementation of the path instead (the
 C restatement of the reference's Jacobi solvers, all host threads), on a
@@ -239,6 +242,104 @@ def error_vs_fp64(mc, t, g, x) -> dict:
             "seconds": round(time.perf_counter() - t0, 2),
             "note": "the benchmark's 5000 Jacobi sweeps are far from converged on an "
                     "800x800 paste; the precision study runs to <= 0.5 LSB"}
+
+
+def reference_cuda(mc, t, g, sysm) -> dict:
+    """The reference's own CUDA solvers on this GPU: its kernels, compiled
+    from its sources (oracle/ref_cuda.py), driven by a restatement of its
+    step loop.  Reports its 5000-sweep step time and residual, and the
+    sweeps and step time the GB300 backend needs to reach the same residual
+    (its kernels update in place, so per sweep they converge faster than
+    Jacobi and only a matched residual compares the two fairly)."""
+    from fpie_gb300 import backend
+    from oracle import cjacobi, ref_cuda
+
+    why = ref_cuda.unavailable_reason()
+    if why:
+        return {"unavailable": why}
+    unknowns = int((mc != 0).sum())
+    r = ref_cuda.RefCudaGrid(8, 8)
+    r.reset(mc, t, g)
+    r.step(SWEEPS)
+    times = []
+    for _ in range(3):
+        r.reset(mc, t, g)
+        t0 = time.perf_counter()
+        r.step(SWEEPS)
+        times.append(time.perf_counter() - t0)
+    ref_s = statistics.median(times)
+    o = cjacobi.CGrid(mc, t, g)
+    o.x = r.state()
+    target = float(o.err64().sum())
+    # Sweeps the GB300 GridSolver needs to reach that residual (steps of
+    # 250 sweeps), then one timed step of that many sweeps from a reset.
+    s = backend.GridSolver(8, 8)
+    s.reset(mc.size, mc, t, g)
+    chunk, done, ours = 250, 0, float("inf")
+    while done < 40 * SWEEPS:
+        _, err = s.step(chunk)
+        done += chunk
+        ours = float(np.asarray(err, np.float64).sum())
+        if ours <= target:
+            break
+    s.reset(mc.size, mc, t, g)
+    s.step(done)
+    mt = []
+    for _ in range(3):
+        s.reset(mc.size, mc, t, g)
+        t0 = time.perf_counter()
+        s.step(done)
+        mt.append(time.perf_counter() - t0)
+    ours_s = statistics.median(mt)
+    line = {
+        "grid": {"value": unknowns * SWEEPS / ref_s, "unit": "pixel-updates/s",
+                 "ms_per_step": ref_s * 1e3, "sweeps": SWEEPS, "residual_sum": target,
+                 "kernel": "iter_grid_kernel, one launch per sweep, 8x8 blocks, in place"},
+        "matched_residual": {"gb300_sweeps": done, "gb300_ms": ours_s * 1e3,
+                             "gb300_residual_sum": ours, "reached": ours <= target,
+                             "reference_ms": ref_s * 1e3,
+                             "note": "GridSolver.step(n) from a reset, n = the first multiple of "
+                                     "250 sweeps whose residual is <= the reference's after 5000"},
+        "note": "the reference's fpie/core/cuda kernels compiled from its sources for sm_103a, "
+                "host step loop restated over the driver API; wall time of step(5000) incl. the "
+                "image and err copies back, median of 3",
+    }
+    if sysm is not None:
+        q = ref_cuda.RefCudaEqu(1024)
+        q.reset(sysm.N, sysm.A, sysm.X, sysm.B)
+        q.step(SWEEPS)
+        et = []
+        for _ in range(3):
+            q.reset(sysm.N, sysm.A, sysm.X, sysm.B)
+            t0 = time.perf_counter()
+            q.step(SWEEPS)
+            et.append(time.perf_counter() - t0)
+        qo = cjacobi.CEqu(sysm.A, sysm.X, sysm.B)
+        qo.X = q.state()
+        qtarget = float(qo.err64().sum())
+        line["equ"] = {"value": (sysm.N - 1) * SWEEPS / statistics.median(et),
+                       "unit": "pixel-updates/s", "ms_per_step": statistics.median(et) * 1e3,
+                       "residual_sum": qtarget,
+                       "kernel": "iter_equ_kernel, one launch per sweep, blocks of 1024, in place"}
+        e = backend.EquSolver(1024)
+        e.reset(sysm.N, sysm.A, sysm.X, sysm.B)
+        edone, eres = 0, float("inf")
+        while edone < 40 * SWEEPS:
+            _, err = e.step(chunk)
+            edone += chunk
+            eres = float(np.asarray(err, np.float64).sum())
+            if eres <= qtarget:
+                break
+        emt = []
+        for _ in range(3):
+            e.reset(sysm.N, sysm.A, sysm.X, sysm.B)
+            t0 = time.perf_counter()
+            e.step(edone)
+            emt.append(time.perf_counter() - t0)
+        line["equ"]["matched_residual"] = {"gb300_sweeps": edone, "gb300_ms": statistics.median(emt) * 1e3,
+                                           "gb300_residual_sum": eres,
+                                           "reached": eres <= qtarget}
+    return line
 
 
 def run_reference(args):
@@ -501,6 +602,7 @@ def run_gb300(args):
         line["cpu_baseline"] = cpu_baseline_grid(mc, t, g)
         if sweeps == SWEEPS:
             line["error_vs_fp64"] = error_vs_fp64(mc, t, g, check.state())
+            line["reference_cuda"] = reference_cuda(mc, t, g, sysm if not args.no_equ else None)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

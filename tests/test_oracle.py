@@ -105,3 +105,21 @@ def test_oracle_catches_a_planted_error():
     a.sweep(5)
     b.sweep(5)
     assert not np.array_equal(a.x, b.x)
+
+
+def test_reference_cuda_harness_builds():
+    """The host side of the reference's CUDA solvers (oracle/ref_cuda_host.c)
+    compiles and exports its entry points; running it needs a GPU."""
+    import shutil
+    import subprocess
+
+    from oracle import ref_cuda
+
+    if not (ref_cuda.cuda_home() / "include" / "cuda.h").is_file() or shutil.which("nm") is None:
+        pytest.skip("no CUDA headers or nm")
+    so = ref_cuda.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(so)], capture_output=True, text=True,
+                         check=True).stdout
+    for sym in ("refcuda_load", "refcuda_grid_sweeps", "refcuda_grid_step", "refcuda_equ_sweeps",
+                "refcuda_equ_step"):
+        assert sym in out, sym
