@@ -140,12 +140,41 @@ def raster_layout(A: np.ndarray):
 
 
 class EquSolver(_Solver):
-    """Jacobi on relabelled unknowns (fpie/core/base_solver.h:12-75)."""
+    """Jacobi on relabelled unknowns (fpie/core/base_solver.h:12-75).
 
-    def __init__(self, block_size: int = 1024) -> None:
+    order "jacobi" (default): the numpy EquSolver's iteration and row-major
+    partition.  order "red_black": the reference's OpenMP EquSolver
+    (fpie/core/openmp/equ.cc): partition numbers odd row+col cells first,
+    then even ones, and each sweep updates the two colours in turn, in place.
+    """
+
+    ORDERS = {"jacobi": 0, "red_black": 1}
+
+    def __init__(self, block_size: int = 1024, order: str = "jacobi") -> None:
         super().__init__()
         self._create("fpie_equ_create", int(block_size))
         self.N = 0
+        if order != "jacobi":
+            self.set_order(order)
+
+    def set_order(self, order: str) -> None:
+        """Iteration order; a change discards the loaded system."""
+        if order not in self.ORDERS:
+            raise ValueError(f"order must be one of {sorted(self.ORDERS)}")
+        _abi.call("fpie_equ_set_order", self._h, self.ORDERS[order])
+
+    @property
+    def order(self) -> str:
+        o, mid = ctypes.c_int(0), ctypes.c_int(0)
+        _abi.call("fpie_equ_order", self._h, ctypes.byref(o), ctypes.byref(mid))
+        return {v: k for k, v in self.ORDERS.items()}[o.value]
+
+    @property
+    def n_mid(self) -> int:
+        """First even id of the last red-black partition (0 if none)."""
+        o, mid = ctypes.c_int(0), ctypes.c_int(0)
+        _abi.call("fpie_equ_order", self._h, ctypes.byref(o), ctypes.byref(mid))
+        return mid.value
 
     def partition(self, mask: np.ndarray) -> np.ndarray:
         m = _as(mask, np.int32, (None, None), "mask")

@@ -89,6 +89,46 @@ __global__ void equ_sweep_kernel(EquGeom E, const int4* __restrict__ A,
   }
 }
 
+// Half a red-black sweep (the reference's OpenMP EquSolver order,
+// fpie/core/openmp/equ.cc:67-80, 109-118): rows lo..hi-1 updated in place as
+// ((((B + X[U]) + X[D]) + X[L]) + X[R]) / 4.  Every neighbour of these rows
+// is of the other colour or row 0 (checked at reset by equ_colour_kernel), so
+// no thread of the launch writes a value another thread reads: the result is
+// the reference's, whatever the thread order.  Plain loads: x is written
+// during the launch (at other addresses).
+__global__ void equ_rb_kernel(EquGeom E, const int4* __restrict__ A,
+                              const float* __restrict__ b, float* x, int lo, int hi) {
+  const int i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  const int4 a = __ldg(A + i);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float* xc = x + c * E.np;
+    float s = __fadd_rn(__ldg(b + c * E.np + i), xc[a.x]);
+    s = __fadd_rn(s, xc[a.y]);
+    s = __fadd_rn(s, xc[a.z]);
+    s = __fadd_rn(s, xc[a.w]);
+    x[c * E.np + i] = __fmul_rn(s, 0.25f);
+  }
+}
+
+// Counts neighbour entries that break the red-black colouring: a row in
+// 1..n_mid-1 (red) must only name rows in n_mid..N-1 or 0, a row in
+// n_mid..N-1 (black) only rows in 1..n_mid-1 or 0.
+__global__ void equ_colour_kernel(EquGeom E, const int4* __restrict__ A, int n_mid,
+                                  unsigned int* __restrict__ bad) {
+  unsigned int nbad = 0;
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < E.N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int4 a = A[i];
+    const bool red = i < n_mid;
+    const int nb[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) nbad += (unsigned)(nb[k] != 0 && (nb[k] < n_mid) == red);
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
 // Residual partials (B + sum X[A] - 4X, numpy order) and the clipped image.
 __global__ void __launch_bounds__(256)
 equ_finish_kernel(EquGeom E, const int4* __restrict__ A,
@@ -131,6 +171,7 @@ void grid_run(Solver* s, cudaStream_t st, int iters);
 void grid_pin_kernel(Solver* s, const std::string& name);
 std::string grid_kernel_of(Solver* s);
 void grid_set_spin(Solver* s, long long spins);
+void grid_set_red_black(Solver* s, bool on);
 
 // Whether the system A (N x 4: up, down, left, right; 0 = the constant row)
 // is a 4-neighbour raster stencil, i.e. its unknowns can be placed on a grid
@@ -142,7 +183,13 @@ void grid_set_spin(Solver* s, long long spins);
 // an unknown.  On success pos[i] (i >= 1) is unknown i's pixel, row-major in
 // an n x m crop: connected components are placed one below the other, a row
 // apart, inside a 1-pixel frame.  Row 0 must be the constant (all-zero A).
-static bool raster_embed(int N, const int32_t* A, std::vector<int>& pos, int& n, int& m) {
+// n_mid > 0 (red-black order): every component is also placed so that its
+// unknowns 1..n_mid-1 land on odd row + col and the others on even (one
+// column further right if needed), the colouring the red-black grid kernel
+// derives from a pixel's position.  The system must already be 2-coloured
+// by n_mid (neighbours of different colours).
+static bool raster_embed(int N, const int32_t* A, std::vector<int>& pos, int& n, int& m,
+                         int n_mid = 0) {
   if (N < 2) return false;
   for (int k = 0; k < 4; ++k)
     if (A[k] != 0) return false;
@@ -180,12 +227,19 @@ static bool raster_embed(int N, const int32_t* A, std::vector<int>& pos, int& n,
         }
       }
     }
+    // The seed s sits at (rows - rmin, 1 - cmin); with a colouring, shift
+    // the component right by one column if s would get the wrong parity.
+    int shift = 0;
+    if (n_mid > 0) {
+      const bool odd = ((rows - rmin) + (1 - cmin)) % 2 != 0;
+      if (odd != (s < n_mid)) shift = 1;
+    }
     for (size_t q = head; q < queue.size(); ++q) {
       R[queue[q]] += (int)(rows - rmin);
-      C[queue[q]] += 1 - cmin;
+      C[queue[q]] += 1 - cmin + shift;
     }
     rows += (long long)(rmax - rmin + 1) + 1;  // the component, then an empty row
-    width = std::max(width, (long long)(cmax - cmin + 1) + 2);
+    width = std::max(width, (long long)(cmax - cmin + 1) + 2 + shift);
     if (rows > (1LL << 30)) return false;
   }
   // The crop must stay comparable to the system (many scattered pieces would
@@ -264,6 +318,15 @@ struct EquSolverImpl : Solver {
   static constexpr int kChunk = 64;
   cudaGraphExec_t chunk[2] = {nullptr, nullptr};
 
+  // ---- iteration order: FPIE_ORDER_JACOBI (numpy) or FPIE_ORDER_RED_BLACK
+  // (the reference's OpenMP EquSolver).  n_mid: the first even id of the
+  // last red-black partition (fpie/core/openmp/equ.cc:42); the state is
+  // updated in place in x[cur].
+  int order = FPIE_ORDER_JACOBI;
+  int n_mid = 0;
+  cudaGraphExec_t rb_chunk = nullptr;
+  int rb_chunk_mid = -1;
+
   // ---- grid mode: systems that are a 4-neighbour raster stencil run on an
   // internal grid solver (its autotuned temporally blocked kernels); the
   // state lives there and is gathered back into x[cur] when needed.
@@ -277,6 +340,7 @@ struct EquSolverImpl : Solver {
   // the device at the next reset of a system of the same size.
   int* d_occ = nullptr;             // unknown id per crop pixel
   int lay_N = 0, lay_n = 0, lay_m = 0;
+  int lay_mid = 0;                  // the colouring it was placed for (0: none)
   long long spin_limit = 1LL << 26;
 
   explicit EquSolverImpl(int block_size) {
@@ -307,6 +371,61 @@ struct EquSolverImpl : Solver {
     for (auto& e : chunk) {
       if (e) cudaGraphExecDestroy(e);
       e = nullptr;
+    }
+    if (rb_chunk) cudaGraphExecDestroy(rb_chunk);
+    rb_chunk = nullptr;
+    rb_chunk_mid = -1;
+  }
+
+  void set_order(int o) {
+    FPIE_REQUIRE(o == FPIE_ORDER_JACOBI || o == FPIE_ORDER_RED_BLACK, FPIE_ERR_ARG,
+                 "order must be FPIE_ORDER_JACOBI or FPIE_ORDER_RED_BLACK");
+    if (o == order) return;
+    cudaStreamSynchronize(stream);
+    order = o;
+    n_mid = 0;
+    ready = false;  // the loaded system was numbered for the other order
+    use_grid = false;
+    grid_newer = false;
+  }
+
+  // ids of a partition: row-major (Jacobi), or odd row+col first, then even
+  // (red-black; fpie/core/openmp/equ.cc:22-56), remembering n_mid.
+  void partition(const int32_t* mask, int n, int m, int32_t* ids) {
+    const long long total = (long long)n * m;
+    int32_t cnt = 0;
+    if (order == FPIE_ORDER_JACOBI) {
+      for (long long k = 0; k < total; ++k) ids[k] = mask[k] > 0 ? ++cnt : 0;
+      return;
+    }
+    for (int parity = 1; parity >= 0; --parity) {
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < m; ++j) {
+          const long long k = (long long)i * m + j;
+          if ((i + j) % 2 == parity) ids[k] = mask[k] > 0 ? ++cnt : 0;
+        }
+      if (parity == 1) n_mid = cnt + 1;
+    }
+  }
+
+  // Red-black: the loaded system must follow the colouring of the last
+  // partition, or the in-place halves would race.
+  void check_colouring() {
+    if (n_mid < 1 || n_mid > E.N) {
+      release();
+      throw Error{FPIE_ERR_STATE, "red-black order: call partition() on the system's mask before "
+                                  "reset (n_mid = " + std::to_string(n_mid) + ", N = " +
+                                  std::to_string(E.N) + ")"};
+    }
+    FPIE_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), stream));
+    equ_colour_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, A, n_mid, d_bad);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(h_bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    if (*h_bad) {
+      release();
+      throw Error{FPIE_ERR_ARG, "red-black order: A holds " + std::to_string(*h_bad) +
+                                    " neighbour(s) of a row's own colour for the last partition"};
     }
   }
 
@@ -345,6 +464,7 @@ struct EquSolverImpl : Solver {
   void enter_grid(int n, int m) {
     if (!grid) grid = new_grid_solver(8, 8);
     grid_set_spin(grid, spin_limit);
+    grid_set_red_black(grid, order == FPIE_ORDER_RED_BLACK);
     if (kernel_req != "auto") grid_pin_kernel(grid, kernel_req);
     grid_reset_from_equ(grid, stream, n, m, E.N, d_pos, x[0], b, E.np);
     use_grid = true;
@@ -352,8 +472,10 @@ struct EquSolverImpl : Solver {
   }
 
   // Whether the last placement fits the system now loaded (device check).
+  int colour_mid() const { return order == FPIE_ORDER_RED_BLACK ? n_mid : 0; }
+
   bool cached_layout_fits() {
-    if (!d_occ || lay_N != E.N || lay_N < 2) return false;
+    if (!d_occ || lay_N != E.N || lay_N < 2 || lay_mid != colour_mid()) return false;
     FPIE_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), stream));
     equ_layout_check_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, A, x[0], b, d_pos, d_occ,
                                                                    lay_m, d_bad);
@@ -368,6 +490,11 @@ struct EquSolverImpl : Solver {
   // on the host, or NULL to fetch it from the device if the search is needed.
   void choose_mode(const int32_t* hA) {
     use_grid = false;
+    if (order == FPIE_ORDER_RED_BLACK) {
+      FPIE_REQUIRE(kernel_req == "auto" || kernel_req == "gather", FPIE_ERR_ARG,
+                   "red-black order runs on its own kernels, not grid kernel '" + kernel_req + "'");
+      check_colouring();
+    }
     if (kernel_req == "gather") return;
     if (cached_layout_fits()) {
       enter_grid(lay_n, lay_m);
@@ -390,7 +517,7 @@ struct EquSolverImpl : Solver {
     for (float v : row0) zero_row0 = zero_row0 && v == 0.f;
     std::vector<int> pos;
     int n = 0, m = 0;
-    const bool ok = zero_row0 && raster_embed(E.N, hA, pos, n, m);
+    const bool ok = zero_row0 && raster_embed(E.N, hA, pos, n, m, colour_mid());
     if (!ok) {
       FPIE_REQUIRE(kernel_req == "auto", FPIE_ERR_ARG,
                    "grid kernel '" + kernel_req + "' needs a 4-neighbour raster system "
@@ -410,6 +537,7 @@ struct EquSolverImpl : Solver {
     lay_N = E.N;
     lay_n = n;
     lay_m = m;
+    lay_mid = colour_mid();
     enter_grid(n, m);
     FPIE_CUDA(cudaStreamSynchronize(stream));  // pos is a host vector
   }
@@ -433,7 +561,7 @@ struct EquSolverImpl : Solver {
   }
 
   std::string kernel_name() const {
-    if (!use_grid) return "gather";
+    if (!use_grid) return order == FPIE_ORDER_RED_BLACK ? "red_black" : "gather";
     return "grid:" + grid_kernel_of(grid);
   }
 
@@ -512,6 +640,9 @@ struct EquSolverImpl : Solver {
                    const uint8_t* tgt, int th, int tw, int s_row, int s_col, int t_row, int t_col,
                    int mode, bool on_device, int* box_out) {
     FPIE_REQUIRE(src && msk && tgt && box_out, FPIE_ERR_ARG, "null input array");
+    FPIE_REQUIRE(order == FPIE_ORDER_JACOBI, FPIE_ERR_STATE,
+                 "reset from images numbers unknowns row-major; red-black order needs "
+                 "partition() + reset()");
     FPIE_REQUIRE(sh > 0 && sw > 0 && mh > 0 && mw > 0 && th > 0 && tw > 0, FPIE_ERR_ARG, "empty image");
     FPIE_REQUIRE(mch == 1 || mch == 3, FPIE_ERR_ARG, "mask must have 1 or 3 channels");
     FPIE_REQUIRE(mode >= 0 && mode <= 2, FPIE_ERR_ARG, "gradient mode must be 0 (src), 1 (avg), 2 (max)");
@@ -626,8 +757,49 @@ struct EquSolverImpl : Solver {
     FPIE_CUDA(e);
   }
 
+  void rb_sweep_once(cudaStream_t st) {
+    if (n_mid > 1)
+      equ_rb_kernel<<<(n_mid - 1 + block - 1) / block, block, 0, st>>>(E, A, b, x[cur], 1, n_mid);
+    if (E.N > n_mid)
+      equ_rb_kernel<<<(E.N - n_mid + block - 1) / block, block, 0, st>>>(E, A, b, x[cur], n_mid, E.N);
+  }
+
+  void run_rb(int iters) {
+    const int per = (n_mid > 1) + (E.N > n_mid);
+    while (iters >= kChunk) {
+      if (!rb_chunk || rb_chunk_mid != n_mid) {
+        if (rb_chunk) cudaGraphExecDestroy(rb_chunk);
+        rb_chunk = nullptr;
+        cudaStream_t cs = nullptr;
+        cudaGraph_t graph = nullptr;
+        FPIE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+          for (int k = 0; k < kChunk; ++k) rb_sweep_once(cs);
+          e = cudaStreamEndCapture(cs, &graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&rb_chunk, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+        FPIE_CUDA(e);
+        rb_chunk_mid = n_mid;
+      }
+      FPIE_CUDA(cudaGraphLaunch(rb_chunk, stream));
+      post_launch(this, kChunk * per);
+      iters -= kChunk;
+    }
+    for (; iters > 0; --iters) {
+      rb_sweep_once(stream);
+      post_launch(this, per);
+    }
+  }
+
   void run_sweeps(int iters) {
     FPIE_REQUIRE(ready, FPIE_ERR_STATE, "step called before reset");
+    if (order == FPIE_ORDER_RED_BLACK && !use_grid) {
+      run_rb(iters);
+      return;
+    }
     if (use_grid) {
       if (iters > 0) {
         grid_run(grid, stream, iters);
@@ -706,12 +878,23 @@ extern "C" {
 int fpie_equ_partition(fpie_solver* s, const int32_t* mask, int n, int m,
                        int32_t* ids_out) {
   return guarded([&] {
-    equ_of(s);
+    EquSolverImpl* h = equ_of(s);
     FPIE_REQUIRE(mask && ids_out, FPIE_ERR_ARG, "null array");
     FPIE_REQUIRE(n >= 0 && m >= 0, FPIE_ERR_ARG, "negative mask shape");
-    int32_t cnt = 0;
-    const long long total = (long long)n * m;
-    for (long long k = 0; k < total; ++k) ids_out[k] = mask[k] > 0 ? ++cnt : 0;
+    h->partition(mask, n, m, ids_out);
+  });
+}
+
+int fpie_equ_set_order(fpie_solver* s, int order) {
+  return guarded([&] { equ_of(s)->set_order(order); });
+}
+
+int fpie_equ_order(fpie_solver* s, int* order, int* n_mid) {
+  return guarded([&] {
+    FPIE_REQUIRE(order != nullptr, FPIE_ERR_ARG, "null output");
+    const EquSolverImpl* h = equ_of(s);
+    *order = h->order;
+    if (n_mid) *n_mid = h->n_mid;
   });
 }
 

@@ -639,7 +639,7 @@ struct GridSolverImpl : Solver {
     const bool listed = tma;  // kernels that take the active-tile list
     const int th = tma ? tma_tile_h() : tb_variants()[variant].tile_h;
     const int tw = tma ? tma_tile_w() : tb_variants()[variant].tile_w;
-    const int kd = tma ? tma_depth() : tb_variants()[variant].depth;
+    const int kd = tma ? tma_depth() : tb_variants()[variant].apron;
     tiles_x = (G.m + tw - 1) / tw;
     tiles = tiles_x * ((G.n + th - 1) / th);
     if (tiles > flags_cap) {
@@ -717,6 +717,29 @@ struct GridSolverImpl : Solver {
       flags_ok = false;
     }
     variant = v;
+  }
+
+  // Red-black sweeps instead of Jacobi: only the EquSolver's red-black
+  // order sets this, on the grid placement of its system.
+  bool red_black = false;
+
+  static int red_black_variant() {
+    for (size_t k = 0; k < tb_variants().size(); ++k)
+      if (tb_variants()[k].red_black) return (int)k;
+    return -100;
+  }
+
+  void set_red_black(bool on) {
+    if (on == red_black) return;
+    red_black = on;
+    if (on) {
+      FPIE_REQUIRE(precision == FPIE_FP32, FPIE_ERR_STATE, "red-black sweeps are FP32 only");
+      select_variant(red_black_variant());
+      pinned = tuned = true;
+    } else {
+      select_variant(default_variant());
+      pinned = tuned = false;
+    }
   }
 
   // k sweeps (k <= depth()) from buffer `from`; flips nothing (caller does).
@@ -1142,6 +1165,9 @@ struct GridSolverImpl : Solver {
   }
 
   void set_kernel(const std::string& name) {
+    FPIE_REQUIRE(!red_black || name == "auto" || name == tb_variants()[red_black_variant()].name,
+                 FPIE_ERR_ARG, "red-black sweeps run on their own kernel, not '" + name + "'");
+    if (red_black) return;  // the red-black kernel stays pinned
     if (name == "auto") {
       pinned = false;
       tuned = false;
@@ -1165,7 +1191,7 @@ struct GridSolverImpl : Solver {
     if (name == "p16w8k16t") v = kTma;
     if (name == "p16w8k16d") v = kFlow;
     for (size_t k = 0; k < tb_variants().size(); ++k)
-      if (name == tb_variants()[k].name) v = (int)k;
+      if (name == tb_variants()[k].name && !tb_variants()[k].red_black) v = (int)k;
     FPIE_REQUIRE(v != -100, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
     select_variant(v);
     pinned = true;
@@ -1183,6 +1209,7 @@ struct GridSolverImpl : Solver {
   void set_precision(int p) {
     FPIE_REQUIRE(p == FPIE_FP32 || p == FPIE_MIXED_FP16 || p == FPIE_MIXED_BF16, FPIE_ERR_ARG,
                  "unknown precision");
+    FPIE_REQUIRE(!red_black || p == FPIE_FP32, FPIE_ERR_STATE, "red-black sweeps are FP32 only");
     if (p != precision) {
       precision = p;
       pinned = false;
@@ -1343,6 +1370,7 @@ void grid_run(Solver* s, cudaStream_t st, int iters) {
 void grid_pin_kernel(Solver* s, const std::string& name) {
   static_cast<GridSolverImpl*>(s)->set_kernel(name);
 }
+void grid_set_red_black(Solver* s, bool on) { static_cast<GridSolverImpl*>(s)->set_red_black(on); }
 std::string grid_kernel_of(Solver* s) { return static_cast<GridSolverImpl*>(s)->kernel_name(); }
 void grid_set_spin(Solver* s, long long spins) {
   GridSolverImpl* h = static_cast<GridSolverImpl*>(s);

@@ -177,6 +177,7 @@ TbVariant make_variant(const char* name) {
   v.rows_per_thread = R;
   v.warps = W;
   v.depth = K;
+  v.apron = K;
   v.tile_h = W * R - 2 * K;
   v.tile_w = 128 - 2 * K;
   v.launch = &launch_tb<R, W, K, GS>;

@@ -9,8 +9,10 @@ namespace fpie {
 
 struct TbVariant {
   const char* name;
-  int rows_per_thread, warps, depth;  // R, W, K
-  int tile_h, tile_w;                 // output tile: W*R - 2K rows, 128 - 2K columns
+  int rows_per_thread, warps, depth;  // R, W, K (sweeps per launch)
+  int tile_h, tile_w;                 // output tile: W*R - 2*apron rows, 128 - 2*apron columns
+  int apron = 0;                      // region border around the tile (K, or 2K for red-black)
+  bool red_black = false;             // red-black sweeps (EquSolver order), not Jacobi
   // Runs ksweeps (<= depth) sweeps xin -> xout on every active tile.
   void (*launch)(const GridGeom& G, const uint8_t* mask, const float* g,
                  const float* xin, float* xout, const uint8_t* active,

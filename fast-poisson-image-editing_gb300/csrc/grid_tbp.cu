@@ -23,7 +23,9 @@
 
 namespace fpie {
 
-template <int R, int W, int K, typename TS, bool ZS, bool GS = false>
+// RB: red-black sweeps (the EquSolver's red-black order on its grid
+// placement); K is then the apron, ksweeps <= K / 2.
+template <int R, int W, int K, typename TS, bool ZS, bool GS = false, bool RB = false>
 __global__ void __launch_bounds__(W * 32)
 grid_tbp_kernel(GridGeom G, const uint8_t* __restrict__ mask,
                 const float* __restrict__ g, const TS* __restrict__ xin,
@@ -48,9 +50,9 @@ grid_tbp_kernel(GridGeom G, const uint8_t* __restrict__ mask,
   TS* oc = xout + c * G.plane;
   float2* sg = reinterpret_cast<float2*>(tbp_dyn) + (size_t)w * (R / 2) * 32 * 4;
   if (flag == 2)
-    tbp_body<R, W, K, true, TS, ZS, false, GS>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
+    tbp_body<R, W, K, true, TS, ZS, false, GS, RB>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
   else
-    tbp_body<R, W, K, false, TS, ZS, false, GS>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
+    tbp_body<R, W, K, false, TS, ZS, false, GS, RB>(G, mask, gc, xc, oc, base, ksweeps, lane, w, edge, sg);
 }
 
 // Fused first launch of a refinement cycle (tbp_fold_body): all channels'
@@ -97,11 +99,11 @@ void prepare_tbp() {
                                    (int)tbp_smem<R, W, GS>()));
 }
 
-template <int R, int W, int K, bool GS = false>
+template <int R, int W, int K, bool GS = false, bool RB = false>
 void launch_tbp(const GridGeom& G, const uint8_t* mask, const float* g,
                 const float* xin, float* xout, const uint8_t* active,
                 int tiles_x, int tiles, int ksweeps, cudaStream_t st) {
-  grid_tbp_kernel<R, W, K, float, false, GS><<<dim3(tiles, 3), W * 32, tbp_smem<R, W, GS>(), st>>>(
+  grid_tbp_kernel<R, W, K, float, false, GS, RB><<<dim3(tiles, 3), W * 32, tbp_smem<R, W, GS>(), st>>>(
       G, mask, g, xin, xout, active, tiles_x, ksweeps);
 }
 
@@ -112,10 +114,29 @@ TbVariant make_packed(const char* name) {
   v.rows_per_thread = R;
   v.warps = W;
   v.depth = K;
+  v.apron = K;
   v.tile_h = W * R - 2 * K;
   v.tile_w = 128 - 2 * K;
   v.launch = &launch_tbp<R, W, K, GS>;
   v.prepare = GS ? &prepare_tbp<R, W, K, GS> : &no_prepare;
+  return v;
+}
+
+// Red-black variant: KS red-black sweeps per launch on tiles with an apron
+// of 2 * KS.
+template <int R, int W, int KS>
+TbVariant make_packed_rb(const char* name) {
+  TbVariant v;
+  v.name = name;
+  v.rows_per_thread = R;
+  v.warps = W;
+  v.depth = KS;
+  v.apron = 2 * KS;
+  v.tile_h = W * R - 4 * KS;
+  v.tile_w = 128 - 4 * KS;
+  v.red_black = true;
+  v.launch = &launch_tbp<R, W, 2 * KS, false, true>;
+  v.prepare = &no_prepare;
   return v;
 }
 
@@ -178,6 +199,7 @@ void append_packed_variants(std::vector<TbVariant>& v) {
   v.push_back(make_packed<16, 8, 4>("p16w8k4"));
   v.push_back(make_packed<12, 12, 8, true>("p12w12k8s"));
   v.push_back(make_packed<8, 16, 8, true>("p8w16k8s"));
+  v.push_back(make_packed_rb<16, 8, 8>("rb16w8k8"));
 }
 
 }  // namespace fpie

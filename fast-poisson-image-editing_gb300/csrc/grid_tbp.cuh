@@ -216,6 +216,86 @@ __device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (
   if (s < ksweeps) tbp_sweep<R, W, FULL, GS, true>(P, Gp, mk, 0, lane, w, edge, sg);
 }
 
+// ---- red-black order (the reference's OpenMP EquSolver, placed on a grid) --
+// A cell's colour is the parity of row + col on the grid; a sweep updates the
+// odd cells (the first half of the equation numbering), then the even ones.
+// Region origins and every warp's first row are even, and a pair row i holds
+// rows i and i + R/2 (same parity), so the cells of column group j in pair
+// row i have parity (i + j) % 2: which registers a half-step updates is
+// fixed at compile time.  An updated cell reads only cells of the other
+// colour, which the half-step leaves alone, so the update is in place and
+// its order is free; each update is ((((g + up) + down) + left) + right) *
+// 0.25 as in every other kernel.  The valid part of a region shrinks by one
+// cell per half-step, so K red-black sweeps need an apron of 2K.
+template <int R, int W, bool FULL, bool ODD>
+__device__ __forceinline__ void tbp_rb_half(float2 (&P)[R / 2][4], const float2 (&Gp)[R / 2][4],
+                                            const uint32_t (&mk)[R], int par, int lane, int w,
+                                            float4 (&edge)[2][2][W][32]) {
+  constexpr int H = R / 2;
+  static_assert(H % 2 == 0, "the two rows of a pair must have the same parity");
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  edge[par][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+  edge[par][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+  __syncthreads();
+  const float4 above = w > 0 ? edge[par][1][w - 1][lane] : zero;
+  const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
+  const float av[4] = {above.x, above.y, above.z, above.w};
+  const float bv[4] = {below.x, below.y, below.z, below.w};
+  const float2 q = make_float2(0.25f, 0.25f);
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const int j0 = (i + (ODD ? 1 : 0)) & 1;  // column groups j0 and j0 + 2 have this colour
+    // The neighbour across the lane boundary: lane-1's group 3 (for j0 = 0)
+    // or lane+1's group 0 (for j0 = 1); all lanes take part in the shuffle.
+    const float2 src = j0 == 0 ? P[i][3] : P[i][0];
+    const float2 nb = j0 == 0 ? make_float2(__shfl_up_sync(0xffffffffu, src.x, 1),
+                                            __shfl_up_sync(0xffffffffu, src.y, 1))
+                              : make_float2(__shfl_down_sync(0xffffffffu, src.x, 1),
+                                            __shfl_down_sync(0xffffffffu, src.y, 1));
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) {
+      const int j = j0 + 2 * jj;
+      const float2 up = i > 0 ? P[i - 1][j] : make_float2(av[j], P[H - 1][j].x);
+      const float2 dn = i < H - 1 ? P[i + 1][j] : make_float2(P[0][j].y, bv[j]);
+      const float2 l = j > 0 ? P[i][j - 1] : nb;
+      const float2 r = j < 3 ? P[i][j + 1] : nb;
+      float2 t = __fadd2_rn(Gp[i][j], up);
+      t = __fadd2_rn(t, dn);
+      t = __fadd2_rn(t, l);
+      t = __fadd2_rn(t, r);
+      const float2 o = __fmul2_rn(t, q);
+      P[i][j] = FULL ? o : pick2(mk[i], mk[i + H], 0xffu << (8 * j), o, P[i][j]);
+    }
+  }
+}
+
+// ksweeps red-black sweeps (odd half, even half) of the strip in P.
+template <int R, int W, bool FULL>
+__device__ __forceinline__ void tbp_rb_sweeps(float2 (&P)[R / 2][4], const float2 (&Gp)[R / 2][4],
+                                              const uint32_t (&mk)[R], int ksweeps, int lane, int w,
+                                              float4 (&edge)[2][2][W][32]) {
+  constexpr int H = R / 2;
+  if (!FULL) {
+    uint32_t any = 0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) any |= mk[i];
+    if (__all_sync(0xffffffffu, any == 0u)) {  // nothing to update: edges and barriers only
+      const float4 top = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+      const float4 bot = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+      for (int h = 0; h < 2 * ksweeps; ++h) {
+        edge[h & 1][0][w][lane] = top;
+        edge[h & 1][1][w][lane] = bot;
+        __syncthreads();
+      }
+      return;
+    }
+  }
+  for (int s = 0; s < ksweeps; ++s) {
+    tbp_rb_half<R, W, FULL, true>(P, Gp, mk, 0, lane, w, edge);
+    tbp_rb_half<R, W, FULL, false>(P, Gp, mk, 1, lane, w, edge);
+  }
+}
+
 // TS: storage type of the swept state (float for the plain solver; __half
 // or __nv_bfloat16 for the correction of the mixed form).  zero_start: the
 // state starts at 0 instead of being loaded (first inner launch of a
@@ -223,7 +303,9 @@ __device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (
 // GS: the grad pairs live in shared memory (sg: this warp's H x 32 x 4
 // float2, i.e. W*R*32*16 bytes per CTA, dynamic) instead of registers,
 // freeing 4R registers per thread for taller regions.
-template <int R, int W, int K, bool FULL, typename TS, bool ZS, bool CG = false, bool GS = false>
+// RB: red-black sweeps (K is then the apron, 2 x the sweeps per launch).
+template <int R, int W, int K, bool FULL, typename TS, bool ZS, bool CG = false, bool GS = false,
+          bool RB = false>
 __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __restrict__ mask,
                                          const float* __restrict__ gc,
                                          const TS* __restrict__ xc, TS* __restrict__ oc,
@@ -262,7 +344,12 @@ __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __res
       mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
     }
   }
-  tbp_sweeps<R, W, FULL, GS>(P, Gp, mk, ksweeps, lane, w, edge, sg);
+  if constexpr (RB) {
+    static_assert(!GS, "red-black sweeps keep grad in registers");
+    tbp_rb_sweeps<R, W, FULL>(P, Gp, mk, ksweeps, lane, w, edge);
+  } else {
+    tbp_sweeps<R, W, FULL, GS>(P, Gp, mk, ksweeps, lane, w, edge, sg);
+  }
   if (lane >= K / 4 && lane < 32 - K / 4) {
 #pragma unroll
     for (int i = 0; i < H; ++i) {

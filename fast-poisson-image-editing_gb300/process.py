@@ -9,7 +9,11 @@ solver's uint8 result into a copy of the target (fpie/process.py:374-381,
 
 Backends (``ALL_BACKEND``, printed by ``--check-backend``):
 
-* ``gb300``      -- plain FP32 Jacobi on the GB300 kernels;
+* ``gb300``      -- plain FP32 Jacobi on the GB300 kernels (the numpy
+                    backend's iteration);
+* ``gb300-rb``   -- the OpenMP backend's iterations: red-black Gauss-Seidel
+                    for the equation method (fpie/core/openmp/equ.cc), Jacobi
+                    for the grid method;
 * ``gb300-fp16`` -- iterative refinement, FP16 correction sweeps;
 * ``gb300-bf16`` -- iterative refinement, BF16 correction sweeps.
 
@@ -40,7 +44,7 @@ def _default_cpu_count() -> int:
 
 
 CPU_COUNT = _default_cpu_count()
-_PRECISION_OF = {"gb300": "fp32", "gb300-fp16": "fp16", "gb300-bf16": "bf16"}
+_PRECISION_OF = {"gb300": "fp32", "gb300-rb": "fp32", "gb300-fp16": "fp16", "gb300-bf16": "bf16"}
 ALL_BACKEND = list(_PRECISION_OF)
 DEFAULT_BACKEND = "gb300"
 
@@ -58,7 +62,10 @@ def _make_core(kind: str, backend: str, block_size: int, grid_x: int, grid_y: in
         return None
     from . import backend as _backend  # the native library loads here
 
-    core = _backend.EquSolver(block_size) if kind == "equ" else _backend.GridSolver(grid_x, grid_y)
+    if kind == "equ":
+        core = _backend.EquSolver(block_size, order="red_black" if backend == "gb300-rb" else "jacobi")
+    else:
+        core = _backend.GridSolver(grid_x, grid_y)
     if _PRECISION_OF[backend] != "fp32":
         core.set_precision(_PRECISION_OF[backend])
     return core

@@ -37,6 +37,16 @@ enum fpie_status {
  * solve for an FP16 / BF16 correction by iterative refinement). */
 enum fpie_precision { FPIE_FP32 = 0, FPIE_MIXED_FP16 = 1, FPIE_MIXED_BF16 = 2 };
 
+/* Iteration order of an EquSolver (fpie_equ_set_order).
+ * FPIE_ORDER_JACOBI: every sweep reads the previous sweep's values -- the
+ *   numpy EquSolver (fpie/np_solver.py:33-41); partition numbers unknowns
+ *   row-major.
+ * FPIE_ORDER_RED_BLACK: the reference's OpenMP EquSolver -- partition
+ *   numbers the cells with odd row + col first, then the even ones
+ *   (fpie/core/openmp/equ.cc:22-56); a sweep updates unknowns 1..n_mid-1 in
+ *   place, then n_mid..N-1 reading the new values (equ.cc:107-118). */
+enum fpie_order { FPIE_ORDER_JACOBI = 0, FPIE_ORDER_RED_BLACK = 1 };
+
 /* Library version as 10000*major + 100*minor + patch. */
 int fpie_version(void);
 
@@ -55,9 +65,24 @@ int fpie_equ_create(int block_size, fpie_solver** out);
 
 /* Replaces EquSolver.partition (fpie/core/cuda/equ.cu:36-54,
  * fpie/np_solver.py:14-16): ids[i][j] = row-major running count of
- * mask > 0 at set pixels, 0 elsewhere. */
+ * mask > 0 at set pixels, 0 elsewhere.  In FPIE_ORDER_RED_BLACK it replaces
+ * OpenMPEquSolver::partition (fpie/core/openmp/equ.cc:22-56): the count runs
+ * over cells with odd i + j first, then even ones, and the solver keeps
+ * n_mid = the first even id for its sweeps. */
 int fpie_equ_partition(fpie_solver* s, const int32_t* mask, int n, int m,
                        int32_t* ids_out);
+
+/* Selects the iteration order (enum fpie_order; default Jacobi).  A change
+ * discards the loaded system: call partition and reset again.  In red-black
+ * order reset checks that every unknown's neighbours have the other colour
+ * for the last partition's n_mid (FPIE_ERR_ARG if not, FPIE_ERR_STATE if no
+ * partition was made), the sweeps run on the equation kernels, and
+ * fpie_equ_reset_images is refused (it numbers unknowns row-major). */
+int fpie_equ_set_order(fpie_solver* s, int order);
+
+/* The current order and, if n_mid is not NULL, the last red-black
+ * partition's n_mid (0 if none). */
+int fpie_equ_order(fpie_solver* s, int* order, int* n_mid);
 
 /* Replaces EquSolver.reset (fpie/core/base_solver.h:27-59 and
  * CudaEquSolver::post_reset, fpie/core/cuda/equ.cu:56-74).  Copies the
@@ -65,9 +90,11 @@ int fpie_equ_partition(fpie_solver* s, const int32_t* mask, int n, int m,
 int fpie_equ_reset(fpie_solver* s, int N, const int32_t* A, const float* X,
                    const float* B);
 
-/* Replaces EquSolver.step (fpie/core/cuda/equ.cu:189-211): runs `iteration`
- * Jacobi sweeps continuing from the current state, then writes the clipped
- * uint8 state x_out[N][3] and the per-channel sum of |residual| err_out[3]. */
+/* Replaces EquSolver.step (fpie/core/cuda/equ.cu:189-211,
+ * fpie/core/openmp/equ.cc:107-125): runs `iteration` sweeps (Jacobi, or
+ * red-black in that order) continuing from the current state, then writes
+ * the clipped uint8 state x_out[N][3] and the per-channel sum of |residual|
+ * err_out[3]. */
 int fpie_equ_step(fpie_solver* s, int iteration, uint8_t* x_out,
                   float* err_out);
 
@@ -171,7 +198,8 @@ int fpie_equ_get_inputs(fpie_solver* s, int32_t* A, float* B);
  * raster stencil.  Applies from the next reset. */
 int fpie_equ_set_kernel(fpie_solver* s, const char* name);
 
-/* Writes "gather" or "grid:<grid kernel>" (NUL-terminated) into buf. */
+/* Writes "gather", "grid:<grid kernel>" or, in red-black order,
+ * "red_black" (NUL-terminated) into buf. */
 int fpie_equ_kernel(fpie_solver* s, char* buf, int len);
 
 /* Spin limit of the grid kernels' bounded waits in grid placement (see

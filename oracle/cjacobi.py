@@ -47,6 +47,8 @@ def lib():
         _lib.oracle_equ_sweeps.argtypes = [c_int, _i32, _f32, _f32, _f32, c_int, c_int]
         _lib.oracle_equ_sweeps.restype = c_int
         _lib.oracle_equ_residual.argtypes = [c_int, _i32, _f32, _f32, _f64]
+        _lib.oracle_equ_rb_sweeps.argtypes = [c_int, c_int, _i32, _f32, _f32, c_int, c_int]
+        _lib.oracle_equ_rb_sweeps.restype = None
     return _lib
 
 
@@ -111,3 +113,16 @@ class CEqu:
         out = np.empty(self.X.shape, np.uint8)
         lib().oracle_clip_u8(self.X.size, self.X, out)
         return out
+
+
+class CEquRedBlack(CEqu):
+    """Red-black Gauss-Seidel (the reference's OpenMP EquSolver order) by the
+    C restatement: rows 1..n_mid-1 then n_mid..N-1, in place."""
+
+    def __init__(self, A, X, B, n_mid: int, nthreads: int | None = None):
+        super().__init__(A, X, B, nthreads)
+        self.n_mid = int(n_mid)
+
+    def sweep(self, k: int) -> None:
+        if k > 0:
+            lib().oracle_equ_rb_sweeps(self.N, self.n_mid, self.A, self.X, self.B, k, self.nthreads)

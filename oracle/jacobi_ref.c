@@ -124,6 +124,30 @@ int oracle_equ_sweeps(int N, const int32_t* A, float* X, float* tmp,
   return cur == X ? 0 : 1;
 }
 
+/* Red-black Gauss-Seidel of the reference's OpenMP EquSolver
+ * (fpie/core/openmp/equ.cc:67-80, 107-118): rows 1..n_mid-1, then rows
+ * n_mid..N-1, each updated in place; X is N x 3 interleaved. */
+void oracle_equ_rb_sweeps(int N, int n_mid, const int32_t* A, float* X, const float* B, int iters,
+                          int threads) {
+  if (threads > 0) omp_set_num_threads(threads);
+  for (int it = 0; it < iters; ++it) {
+    for (int half = 0; half < 2; ++half) {
+      const int lo = half ? n_mid : 1, hi = half ? N : n_mid;
+#pragma omp parallel for schedule(static)
+      for (int i = lo; i < hi; ++i) {
+        const int32_t* a = A + (int64_t)i * 4;
+        for (int c = 0; c < 3; ++c) {
+          float s = B[(int64_t)i * 3 + c] + X[(int64_t)a[0] * 3 + c];
+          s = s + X[(int64_t)a[1] * 3 + c];
+          s = s + X[(int64_t)a[2] * 3 + c];
+          s = s + X[(int64_t)a[3] * 3 + c];
+          X[(int64_t)i * 3 + c] = s / 4.0f;
+        }
+      }
+    }
+  }
+}
+
 void oracle_equ_residual(int N, const int32_t* A, const float* X,
                          const float* B, double* err) {
   double e0 = 0, e1 = 0, e2 = 0;

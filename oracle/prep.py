@@ -83,16 +83,29 @@ def grid_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, mode):
     return mc, t, grad, box
 
 
-def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, mode):
-    """Return dict with ids, A int32[N,4], X f32[N,3], B f32[N,3], N, and target pixel indices."""
+def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, mode, order: str = "row"):
+    """Return dict with ids, A int32[N,4], X f32[N,3], B f32[N,3], N, and target pixel indices.
+
+    order "row": ids row-major (np_solver / core_cuda partition); "red_black":
+    the OpenMP EquSolver's odd-then-even ids (fpie/core/openmp/equ.cc:22-56),
+    with n_mid = the first even id in the result."""
     m01 = threshold_mask(mask)
     x0, x1, y0, y1 = crop_box(m01)
     mc = m01[x0:x1, y0:y1]
     n, m = mc.shape
-    ids = np.zeros((n, m), np.int64)
-    flat = mc.reshape(-1) > 0
-    ids.reshape(-1)[flat] = np.arange(1, int(flat.sum()) + 1)
-    px, py = np.nonzero(mc)  # row-major, i.e. in id order
+    n_mid = None
+    if order == "red_black":
+        from .np_jacobi import red_black_ids
+
+        ids, n_mid = red_black_ids(mc)
+    else:
+        assert order == "row", order
+        ids = np.zeros((n, m), np.int64)
+        flat = mc.reshape(-1) > 0
+        ids.reshape(-1)[flat] = np.arange(1, int(flat.sum()) + 1)
+    px, py = np.nonzero(mc)
+    sel = np.argsort(ids[px, py], kind="stable")  # unknowns in id order
+    px, py = px[sel], py[sel]
     N = px.size + 1
     so = (mask_on_src[0] + x0, mask_on_src[1] + y0)
     to = (mask_on_tgt[0] + x0, mask_on_tgt[1] + y0)
@@ -121,4 +134,5 @@ def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, mode):
         "N": N,
         "tgt_index": (px + to[0], py + to[1]),
         "mask": mc,
+        "n_mid": n_mid,
     }

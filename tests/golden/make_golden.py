@@ -57,10 +57,16 @@ def run_case(P, name, src, mask, tgt, mos, mot, gradient, checkpoints, omp=False
     ids = e.core.partition(mc)
     ids[mc == 0] = 0
     out["equ_ids"] = ids.astype(np.int32)
-    go = None
+    go = eo = None
     if omp and "openmp" in P.ALL_BACKEND:
         go = P.GridProcessor(gradient=gradient, backend="openmp", n_cpu=4, grid_x=omp_grid[0], grid_y=omp_grid[1])
         go.reset(src, mask, tgt.copy(), mos, mot)
+        # The OpenMP EquSolver: red-black Gauss-Seidel on odd-then-even ids.
+        eo = P.EquProcessor(gradient=gradient, backend="openmp", n_cpu=4)
+        eo.reset(src, mask, tgt.copy(), mos, mot)
+        rb = np.asarray(eo.core.partition(mc)).astype(np.int32)  # same mask: same n_mid
+        rb[mc == 0] = 0
+        out["omp_equ_ids"] = rb
     # Images are stored as the solver-updated crop of the target only.
     x0, x1, y0, y1 = g.x0, g.x1, g.y0, g.y1
     done = 0
@@ -79,6 +85,9 @@ def run_case(P, name, src, mask, tgt, mos, mot, gradient, checkpoints, omp=False
             img, err = go.step(k - done)
             out[f"omp_img_{k}"] = img[x0:x1, y0:y1].copy()
             out[f"omp_err_{k}"] = np.asarray(err, np.float32)
+            img, err = eo.step(k - done)
+            out[f"omp_equ_img_{k}"] = img[x0:x1, y0:y1].copy()
+            out[f"omp_equ_err_{k}"] = np.asarray(err, np.float32)
         done = k
     np.savez_compressed(HERE / f"{name}.npz", **out)
     print(f"{name}: grid crop {mc.shape}, N={N}, checkpoints {checkpoints}")
@@ -119,14 +128,14 @@ def main() -> None:
     mask3[10:14, 6:9] = (128, 128, 127)   # sum 383: off
     mask3[15:19, 10:13] = (128, 128, 128)  # sum 384: on
     mask3[20:22, 2:4] = 255
-    run_case(P, "avg_offsets", src, mask3, tgt, (5, 7), (4, 9), "avg", [3, 40])
+    run_case(P, "avg_offsets", src, mask3, tgt, (5, 7), (4, 9), "avg", [3, 40], omp=True)
 
     # 5. 'src' gradient with a random blob mask reaching the frame.
     rng = np.random.default_rng(2)
     src = rng.integers(0, 256, size=(40, 40, 3), dtype=np.uint8)
     tgt = rng.integers(0, 256, size=(40, 40, 3), dtype=np.uint8)
     mask = (rng.random((40, 40)) > 0.3).astype(np.uint8) * 255
-    run_case(P, "blob_frame", src, mask, tgt, (0, 0), (0, 0), "src", [7, 70])
+    run_case(P, "blob_frame", src, mask, tgt, (0, 0), (0, 0), "src", [7, 70], omp=True)
 
     # 6. Solver level, mask set on the crop border: neighbours outside the
     #    grid contribute nothing (numpy semantics of np_solver.GridSolver).

@@ -66,7 +66,7 @@ def test_empty_mask_and_bad_offsets_raise():
 
 
 def test_backend_list_and_invalid_backend(capsys):
-    assert process.ALL_BACKEND == ["gb300", "gb300-fp16", "gb300-bf16"]
+    assert process.ALL_BACKEND == ["gb300", "gb300-rb", "gb300-fp16", "gb300-bf16"]
     assert process.DEFAULT_BACKEND == "gb300"
     with pytest.raises(AssertionError):
         process.GridProcessor(backend="numpy")

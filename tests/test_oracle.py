@@ -71,6 +71,52 @@ def test_equ_jacobi_matches_reference(golden, impl):
     np.testing.assert_array_equal(state, d[f"equ_state_{cps[-1]}"])
 
 
+OMP_EQU_CASES = ["rand24", "circle256", "avg_offsets", "blob_frame"]
+
+
+@pytest.mark.parametrize("name", OMP_EQU_CASES)
+@pytest.mark.parametrize("impl", ["numpy", "c"])
+def test_red_black_matches_reference_openmp(name, impl):
+    """The red-black restatement against the reference's compiled OpenMP
+    EquSolver: its odd-then-even ids exactly, its uint8 images exactly at
+    every checkpoint, its float32 err within rtol 1e-5 (it sums in float32
+    sequentially; the oracle's sum is float64)."""
+    d = load_golden(name)
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    e = prep.equ_inputs(src, mask, tgt, mos, mot, grad, order="red_black")
+    np.testing.assert_array_equal(e["ids"], d["omp_equ_ids"])
+    cls = np_jacobi.EquRedBlack if impl == "numpy" else cjacobi.CEquRedBlack
+    o = cls(e["A"], e["X"], e["B"], e["n_mid"])
+    idx = e["tgt_index"]
+    x0, x1, y0, y1 = (int(v) for v in d["grid_box"])
+    done = 0
+    for k in (int(v) for v in d["checkpoints"]):
+        o.sweep(k - done)
+        done = k
+        ref = d[f"omp_equ_img_{k}"]
+        np.testing.assert_array_equal(o.image()[1:], ref[idx[0] - x0, idx[1] - y0])
+        np.testing.assert_allclose(o.err64(), d[f"omp_equ_err_{k}"], rtol=1e-5, atol=1e-2)
+
+
+def test_red_black_numpy_equals_c_and_differs_from_jacobi():
+    d = load_golden("circle256")
+    e = prep.equ_inputs(*problem_args(d), order="red_black")
+    a = np_jacobi.EquRedBlack(e["A"], e["X"], e["B"], e["n_mid"])
+    b = cjacobi.CEquRedBlack(e["A"], e["X"], e["B"], e["n_mid"])
+    j = np_jacobi.EquJacobi(e["A"], e["X"], e["B"])
+    for o in (a, b, j):
+        o.sweep(40)
+    np.testing.assert_array_equal(a.X, b.X)
+    assert a.err64().sum() < j.err64().sum()
+
+
+def test_red_black_rejects_same_colour_neighbours():
+    d = load_golden("rand24")
+    e = prep.equ_inputs(*problem_args(d), order="red_black")
+    with pytest.raises(AssertionError):
+        np_jacobi.EquRedBlack(e["A"], e["X"], e["B"], e["n_mid"] + 1)
+
+
 def test_grid_border_semantics():
     """Set pixels on the grid border: outside neighbours contribute nothing."""
     d = load_golden("grid_border")
