@@ -491,7 +491,8 @@ struct EquSolverImpl : Solver {
   void choose_mode(const int32_t* hA) {
     use_grid = false;
     if (order == FPIE_ORDER_RED_BLACK) {
-      FPIE_REQUIRE(kernel_req == "auto" || kernel_req == "gather", FPIE_ERR_ARG,
+      FPIE_REQUIRE(kernel_req == "auto" || kernel_req == "gather" || kernel_req.rfind("rb", 0) == 0,
+                   FPIE_ERR_ARG,
                    "red-black order runs on its own kernels, not grid kernel '" + kernel_req + "'");
       check_colouring();
     }

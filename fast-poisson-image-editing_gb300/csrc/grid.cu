@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <utility>
 
@@ -282,9 +283,10 @@ struct GridSolverImpl : Solver {
     ensure_flow_tables();
     FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
     launch_flow(G, mask, g, x[0], x[1], cur, ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles,
-                iters, d_tma_err, r_spin_limit, flow_grid, stream);
+                iters, d_tma_err, r_spin_limit, flow_grid, stream, red_black);
     post_launch(this);
-    const int levels = (iters + flow_depth() - 1) / flow_depth();
+    const int per_level = red_black ? flow_rb_depth() : flow_depth();
+    const int levels = (iters + per_level - 1) / per_level;
     if (levels & 1) cur ^= 1;
   }
 
@@ -731,15 +733,10 @@ struct GridSolverImpl : Solver {
 
   void set_red_black(bool on) {
     if (on == red_black) return;
+    FPIE_REQUIRE(!on || precision == FPIE_FP32, FPIE_ERR_STATE, "red-black sweeps are FP32 only");
     red_black = on;
-    if (on) {
-      FPIE_REQUIRE(precision == FPIE_FP32, FPIE_ERR_STATE, "red-black sweeps are FP32 only");
-      select_variant(red_black_variant());
-      pinned = tuned = true;
-    } else {
-      select_variant(default_variant());
-      pinned = tuned = false;
-    }
+    select_variant(on ? red_black_variant() : default_variant());
+    pinned = tuned = false;
   }
 
   // k sweeps (k <= depth()) from buffer `from`; flips nothing (caller does).
@@ -788,8 +785,8 @@ struct GridSolverImpl : Solver {
     static std::mutex mu;
     return mu;
   }
-  static std::map<std::pair<int, int>, int>& tune_cache() {
-    static std::map<std::pair<int, int>, int> c;
+  static std::map<std::tuple<int, int, bool>, int>& tune_cache() {
+    static std::map<std::tuple<int, int, bool>, int> c;
     return c;
   }
   static constexpr int kTuneReps = 2;
@@ -797,7 +794,7 @@ struct GridSolverImpl : Solver {
   int autotune(int iters) {
     {
       std::lock_guard<std::mutex> lk(tune_mutex());
-      auto it = tune_cache().find({G.n, G.m});
+      auto it = tune_cache().find({G.n, G.m, red_black});
       if (it != tune_cache().end()) {
         select_variant(it->second);
         tuned = true;
@@ -810,7 +807,7 @@ struct GridSolverImpl : Solver {
     // on any measured shape; timing them would only lengthen the first step.
     std::vector<int> cands;
     for (int v = 0; v < (int)tb_variants().size(); ++v)
-      if (tb_variants()[v].name[0] == 'p') cands.push_back(v);
+      if (red_black ? tb_variants()[v].red_black : tb_variants()[v].name[0] == 'p') cands.push_back(v);
     const int ncand = (int)cands.size();
     if (iters < (ncand + 1) * (kTuneReps + 1) * kChunk + kChunk) return 0;
     cudaEvent_t e0, e1;
@@ -858,8 +855,8 @@ struct GridSolverImpl : Solver {
       }
       check_tma();
     }
-    // The resident kernel, when every active tile fits co-resident.
-    if (build_resident() && r_nctas > 0 && iters - used >= (kTuneReps + 1) * kChunk) {
+    // The resident kernel (Jacobi only), when every active tile fits co-resident.
+    if (!red_black && build_resident() && r_nctas > 0 && iters - used >= (kTuneReps + 1) * kChunk) {
       select_variant(kResident);
       run_resident(kChunk);
       used += kChunk;
@@ -882,7 +879,7 @@ struct GridSolverImpl : Solver {
     select_variant(best);
     tuned = true;
     std::lock_guard<std::mutex> lk(tune_mutex());
-    tune_cache()[{G.n, G.m}] = best;
+    tune_cache()[{G.n, G.m, red_black}] = best;
     return used;
   }
 
@@ -1165,14 +1162,19 @@ struct GridSolverImpl : Solver {
   }
 
   void set_kernel(const std::string& name) {
-    FPIE_REQUIRE(!red_black || name == "auto" || name == tb_variants()[red_black_variant()].name,
-                 FPIE_ERR_ARG, "red-black sweeps run on their own kernel, not '" + name + "'");
-    if (red_black) return;  // the red-black kernel stays pinned
+    if (red_black && name != "auto") {
+      const std::string launch = tb_variants()[red_black_variant()].name;
+      FPIE_REQUIRE(name == launch || name == launch + "d", FPIE_ERR_ARG,
+                   "red-black sweeps run on " + launch + " or " + launch + "d, not '" + name + "'");
+      select_variant(name == launch ? red_black_variant() : kFlow);
+      pinned = true;
+      return;
+    }
     if (name == "auto") {
       pinned = false;
       tuned = false;
       std::lock_guard<std::mutex> lk(tune_mutex());
-      tune_cache().erase({G.n, G.m});
+      tune_cache().erase({G.n, G.m, red_black});
       return;
     }
     if (precision != FPIE_FP32) {
@@ -1202,6 +1204,7 @@ struct GridSolverImpl : Solver {
       return mvariant == kFlow ? std::string("p16w8k16d") : std::string(mixed_variants()[mvariant].name);
     if (variant == kResident) return std::string("res16w8k4");
     if (variant == kTma) return std::string("p16w8k16t");
+    if (variant == kFlow && red_black) return std::string(tb_variants()[red_black_variant()].name) + "d";
     if (variant == kFlow) return std::string("p16w8k16d");
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }

@@ -64,6 +64,7 @@ struct FlowArgs {
   int* error;
   int tiles_x, sweeps, parity;
   long long spin_limit;
+  int red_black;         // red-black sweeps: kK / 2 per level, same tiles and apron
 };
 
 __device__ __forceinline__ FlowRec load_rec(const FlowRec* r) {
@@ -127,6 +128,21 @@ __device__ __noinline__ void flow_item(const FlowArgs& A, int tile, int c, int z
                                                  A.x[pin ^ 1] + co, base, ks, lane, w, edge);
 }
 
+// One item of the red-black order (the EquSolver's grid placement): kK / 2
+// red-black sweeps on the same region, apron kK.  Out of line like flow_item.
+template <bool FULL>
+__device__ __noinline__ void flow_rb_item(const FlowArgs& A, int tile, int c, int z,
+                                          float4 (&edge)[2][2][kW][32], int lane, int w) {
+  const GridGeom& G = A.G;
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long co = c * G.plane;
+  const int pin = (A.parity + z) & 1;
+  const int ks = min(kK / 2, A.sweeps - z * (kK / 2));
+  tbp_body<kR, kW, kK, FULL, float, false, true, false, true>(
+      G, A.mask, A.g + co, A.x[pin] + co, A.x[pin ^ 1] + co, base, ks, lane, w, edge);
+}
+
 // Thread 0 keeps the next item's record and counters, loaded right after
 // the current item's sweeps so that their latency overlaps the release
 // fence and barrier; the other threads get tile and flag through shared
@@ -178,7 +194,8 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
   __shared__ int s_stop, s_tile, s_flag;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int per = 3 * A.list[-1];
-  const int levels = MIXED ? mixed_levels(A.sweeps, kK) : (A.sweeps + kK - 1) / kK;
+  const int per_level = A.red_black ? kK / 2 : kK;
+  const int levels = MIXED ? mixed_levels(A.sweeps, kK) : (A.sweeps + per_level - 1) / per_level;
   const long long total = (long long)levels * per;
   FlowRec R{};
   int v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -207,6 +224,11 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
         flow_mixed_item<true, TS>(A, tile, c, z, edge, lane, w);
       else
         flow_mixed_item<false, TS>(A, tile, c, z, edge, lane, w);
+    } else if (A.red_black) {
+      if (s_flag == 2)
+        flow_rb_item<true>(A, tile, c, z, edge, lane, w);
+      else
+        flow_rb_item<false>(A, tile, c, z, edge, lane, w);
     } else if (s_flag == 2) {
       flow_item<true>(A, tile, c, z, edge, lane, w);
     } else {
@@ -257,6 +279,7 @@ __global__ void flow_rec_kernel(const int* __restrict__ list, const int* __restr
 int flow_tile_h() { return kTH; }
 int flow_tile_w() { return kTW; }
 int flow_depth() { return kK; }
+int flow_rb_depth() { return kK / 2; }
 
 int flow_ctas() {
   int dev = 0, sms = 0, per_sm = 0;
@@ -285,13 +308,14 @@ size_t flow_rec_bytes() { return sizeof(FlowRec); }
 
 void launch_flow(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
                  int parity, const int* list, const void* rec, int* done, int tiles_x, int tiles,
-                 int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st) {
+                 int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st,
+                 bool red_black) {
   FPIE_REQUIRE(sweeps >= 1, FPIE_ERR_ARG, "flow sweep kernel: at least one sweep");
   FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
                "flow sweep kernel: bad tiling");
   FlowArgs a{G, mask, g, {x0, x1}, {nullptr, nullptr}, nullptr, list + 1,
              static_cast<const FlowRec*>(rec), done, error, tiles_x, sweeps, parity & 1,
-             spin_limit};
+             spin_limit, red_black ? 1 : 0};
   void* args[] = {&a};
   FPIE_CUDA(cudaLaunchCooperativeKernel((const void*)grid_flow_kernel<float>, dim3(ctas),
                                         dim3(kW * 32), args, 0, st));
@@ -305,7 +329,7 @@ void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, f
   FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
                "flow sweep kernel: bad tiling");
   FlowArgs a{G, mask, g, {x0, x1}, {e0, e1}, r, list + 1, static_cast<const FlowRec*>(rec), done,
-             error, tiles_x, sweeps, parity & 1, spin_limit};
+             error, tiles_x, sweeps, parity & 1, spin_limit, 0};
   void* args[] = {&a};
   const void* k = bf16 ? (const void*)grid_flow_kernel<__nv_bfloat16>
                        : (const void*)grid_flow_kernel<__half>;

@@ -11,6 +11,7 @@ namespace fpie {
 int flow_tile_h();
 int flow_tile_w();
 int flow_depth();
+int flow_rb_depth();  // red-black sweeps per level (same tiles and apron)
 
 // CTAs of a launch: every SM's share, all co-resident.
 int flow_ctas();
@@ -24,12 +25,14 @@ void launch_flow_tables(const int* list, const uint8_t* flags, int tiles_x, int 
 size_t flow_rec_bytes();
 
 // `sweeps` sweeps on every active tile, from buffer `parity` of {x0, x1};
-// the result is in buffer (parity + ceil(sweeps / 16)) & 1.  done (3 ints
-// per active tile) must be zero.  A neighbourhood wait that exceeds
-// spin_limit polls sets *error to 1 and the launch stops early.
+// the result is in buffer (parity + ceil(sweeps / 16)) & 1 (red_black:
+// red-black sweeps, ceil(sweeps / 8)).  done (3 ints per active tile) must
+// be zero.  A neighbourhood wait that exceeds spin_limit polls sets *error
+// to 1 and the launch stops early.
 void launch_flow(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
                  int parity, const int* list, const void* rec, int* done, int tiles_x, int tiles,
-                 int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st);
+                 int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st,
+                 bool red_black = false);
 
 // The mixed forms (FP16 / BF16 correction, FP32 residual every 64 sweeps)
 // as one launch: the level schedule of the batched kernel (mixed_levels),

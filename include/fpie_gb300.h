@@ -198,8 +198,11 @@ int fpie_equ_get_inputs(fpie_solver* s, int32_t* A, float* B);
  * raster stencil.  Applies from the next reset. */
 int fpie_equ_set_kernel(fpie_solver* s, const char* name);
 
-/* Writes "gather", "grid:<grid kernel>" or, in red-black order,
- * "red_black" (NUL-terminated) into buf. */
+/* Writes "gather", "grid:<grid kernel>" or, in red-black order on the
+ * equation kernels, "red_black" (NUL-terminated) into buf.  The red-black
+ * grid kernels are "rb16w8k8" (8 red-black sweeps per launch) and
+ * "rb16w8k8d" (the whole step in one dependency-flow launch); in red-black
+ * order fpie_equ_set_kernel accepts "auto", "gather" and these two. */
 int fpie_equ_kernel(fpie_solver* s, char* buf, int len);
 
 /* Spin limit of the grid kernels' bounded waits in grid placement (see

@@ -39,7 +39,8 @@ def test_partition_matches_reference_openmp(backend, name):
     assert s.n_mid == n_mid and s.order == "red_black"
 
 
-KERNELS = {"auto": "grid:rb16w8k8", "gather": "red_black"}
+KERNELS = {"auto": "grid:rb16w8k8", "gather": "red_black", "rb16w8k8": "grid:rb16w8k8",
+           "rb16w8k8d": "grid:rb16w8k8d"}
 
 
 @pytest.mark.parametrize("kernel", sorted(KERNELS))
