@@ -12,10 +12,12 @@ the CUDA driver API, compiled here with gcc on first use.
 The reference's CUDA kernels update in place (each sweep reads neighbours
 that other threads of the same launch may already have updated), so they
 are not Jacobi: results differ from run to run and converge faster per
-sweep than Jacobi.  They are compared with the GB300 backend on time per
-sweep and on time to the same residual, never bit for bit.
+sweep than Jacobi.  They are compared with the GB300 backend on time to the
+same error against the converged solution and to the same residual sum,
+never bit for bit.
 
-Only tests and bench.py's baseline legs use this module.
+Only tests, bench.py's baseline legs and the profiling entry point at the
+end of this file (python -m oracle.ref_cuda) use this module.
 """
 
 from __future__ import annotations
@@ -192,3 +194,44 @@ class RefCudaEqu:
 
     def state(self) -> np.ndarray:
         return self.X.cpu().numpy()
+
+
+def _main() -> None:
+    """Runs the reference's CUDA GridSolver (and EquSolver) steps on the
+    square800 workload, for timing and profiling the reference's kernels:
+    python -m oracle.ref_cuda --sweeps N [--equ]."""
+    import argparse
+    import sys
+    import time
+
+    root = pathlib.Path(__file__).resolve().parent.parent
+    sys.path.insert(0, str(root))
+    from fpie_gb300 import backend, prep, workloads
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--sweeps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--equ", action="store_true", help="the EquSolver instead of the GridSolver")
+    a = ap.parse_args()
+    pb = workloads.square800(a.sweeps)
+    if a.equ:
+        sysm = prep.equ_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt, pb.gradient,
+                               backend.EquSolver(1024).partition)
+        s = RefCudaEqu(1024)
+        reset = lambda: s.reset(sysm.N, sysm.A, sysm.X, sysm.B)  # noqa: E731
+    else:
+        mc, t, g, _ = prep.grid_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt,
+                                       pb.gradient)
+        s = RefCudaGrid(8, 8)
+        reset = lambda: s.reset(mc, t, g)  # noqa: E731
+    for k in range(a.steps):
+        reset()
+        t0 = time.perf_counter()
+        _, err = s.step(a.sweeps)
+        dt = time.perf_counter() - t0
+        print(f"step {k}: {a.sweeps} sweeps in {dt * 1e3:.2f} ms ({dt / a.sweeps * 1e6:.2f} us/sweep), "
+              f"err {err.tolist()}")
+
+
+if __name__ == "__main__":
+    _main()
