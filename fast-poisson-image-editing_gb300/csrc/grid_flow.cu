@@ -27,9 +27,10 @@
 // done with their level-z items go on to level z + 1 items whose
 // neighbourhoods are ready instead of idling until the whole level ends.
 #include <algorithm>
+#include <atomic>
+#include <type_traits>
 
 #include "common.cuh"
-#include <type_traits>
 
 #include "grid_flow.cuh"
 #include "grid_tbp.cuh"
@@ -282,8 +283,13 @@ int flow_depth() { return kK; }
 int flow_rb_depth() { return kK / 2; }
 
 int flow_ctas() {
+  // Occupancy queries cost tens of microseconds; the answer is fixed per
+  // device, and every reset rebuilds the flow tables.
+  static std::atomic<int> cached[64];
   int dev = 0, sms = 0, per_sm = 0;
   FPIE_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && cached[dev].load(std::memory_order_relaxed) > 0)
+    return cached[dev].load(std::memory_order_relaxed);
   FPIE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int m = 1 << 30;
   const void* ks[3] = {(const void*)grid_flow_kernel<float>, (const void*)grid_flow_kernel<__half>,
@@ -293,6 +299,7 @@ int flow_ctas() {
     m = std::min(m, per_sm);
   }
   FPIE_REQUIRE(m >= 1, FPIE_ERR_CUDA, "the flow sweep kernel does not fit on an SM");
+  if (dev >= 0 && dev < 64) cached[dev].store(sms * m, std::memory_order_relaxed);
   return sms * m;
 }
 

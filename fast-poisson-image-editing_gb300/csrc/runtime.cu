@@ -1,6 +1,7 @@
 // Library-wide pieces of the C ABI: version, last-error string, device count,
 // stream/precision setters, destroy, and the fixed-order residual finalizer.
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -34,6 +35,28 @@ finalize_kernel(const double* __restrict__ parts, int nparts,
 void launch_finalize(const double* parts, int nparts, float* err,
                      cudaStream_t st) {
   finalize_kernel<<<1, 256, 0, st>>>(parts, nparts, err);
+}
+
+cudaMemPool_t scratch_pool() {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  FPIE_CUDA(cudaGetDevice(&dev));
+  FPIE_REQUIRE(dev >= 0 && dev < 64, FPIE_ERR_STATE, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    FPIE_CUDA(cudaMemPoolCreate(&p, &props));
+    uint64_t keep = 4ULL << 30;
+    FPIE_CUDA(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep));
+    pools[dev] = p;
+  }
+  return pools[dev];
 }
 
 }  // namespace fpie
