@@ -55,6 +55,8 @@ struct BQueue {
   const int2* tiles;       // (tile index, flag) per job, concatenated
   int nlevels;
   int njobs;
+  int ntiles;              // entries of `tiles`
+  int smem_tables;         // job records and tile entries are copied to dynamic shared memory
   unsigned long long* next;
   int* done;
   int* error;
@@ -110,8 +112,14 @@ batch_persistent_kernel(BQueue Q) {
   __shared__ int s_stop;
   __shared__ int2 s_tf;
   // The current item's job record, copied by warp 0 (one round trip) so
-  // that the CTA does not chase it field by field through global memory.
+  // that the CTA does not chase it field by field through global memory --
+  // unless every job record (and tile entry) was copied to dynamic shared
+  // memory at the start (Q.smem_tables), which takes both round trips off
+  // every item's critical path.
   __shared__ __align__(16) BJobDev s_job;
+  extern __shared__ __align__(16) unsigned char batch_dyn[];
+  BJobDev* s_jobs = reinterpret_cast<BJobDev*>(batch_dyn);
+  int2* s_tiles = reinterpret_cast<int2*>(batch_dyn + sizeof(BJobDev) * (size_t)Q.njobs);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const bool fits = Q.nlevels <= kSL && Q.njobs <= kSJ;
   if (fits) {
@@ -119,6 +127,14 @@ batch_persistent_kernel(BQueue Q) {
     for (int k = threadIdx.x; k < Q.nlevels; k += blockDim.x) s_act[k] = Q.act[k];
     for (int k = threadIdx.x; k <= Q.njobs; k += blockDim.x) s_ct[k] = Q.ct[k];
     for (int k = threadIdx.x; k < Q.njobs; k += blockDim.x) s_order[k] = Q.order[k];
+  }
+  if (Q.smem_tables) {
+    static_assert(sizeof(BJobDev) % 4 == 0, "job record in words");
+    const int words = (int)(sizeof(BJobDev) / 4) * Q.njobs;
+    const int* src = reinterpret_cast<const int*>(Q.jobs);
+    int* dst = reinterpret_cast<int*>(s_jobs);
+    for (int k = threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
+    for (int k = threadIdx.x; k < Q.ntiles; k += blockDim.x) s_tiles[k] = Q.tiles[k];
   }
   const long long* lo = fits ? s_lo : Q.lo;
   const long long* ct = fits ? s_ct : Q.ct;
@@ -136,16 +152,16 @@ batch_persistent_kernel(BQueue Q) {
     const int j = order[js];
     const int tc = (int)(i - ct[js]);
     const int ti = tc / 3, c = tc - 3 * ti;
-    if (w == 0) {
-      static_assert(sizeof(BJobDev) % 4 == 0, "job record in words");
+    if (w == 0 && !Q.smem_tables) {
       const int* src = reinterpret_cast<const int*>(Q.jobs + j);
       int* dst = reinterpret_cast<int*>(&s_job);
       for (int k = lane; k < (int)(sizeof(BJobDev) / 4); k += 32) dst[k] = src[k];
       __syncwarp();
     }
-    const BJobDev& J = s_job;
+    const BJobDev& J = Q.smem_tables ? s_jobs[j] : s_job;
+    unsigned long long nxt = 0;
     if (threadIdx.x == 0) {
-      s_tf = Q.tiles[J.tile_off + ti];
+      s_tf = Q.smem_tables ? s_tiles[J.tile_off + ti] : Q.tiles[J.tile_off + ti];
       const int need = J.ntiles * 3 * z;
       long long spins = 0;
       int stop = 0;
@@ -160,6 +176,12 @@ batch_persistent_kernel(BQueue Q) {
       }
       __threadfence();
       s_stop = stop;
+      // The next item is taken now, so that the atomic's round trip
+      // overlaps this item's sweeps.  (A CTA then holds two items; the
+      // lowest unfinished item is always one being worked on, since a held
+      // next item is higher than its CTA's current one, and it waits only
+      // for lower items: no deadlock.)
+      if (!stop) nxt = atomicAdd(Q.next, 1ULL);
     }
     __syncthreads();
     if (s_stop) break;
@@ -214,12 +236,6 @@ batch_persistent_kernel(BQueue Q) {
                         ty * TH, tx * TW, TH, TW);
       }
     }
-    // The next item is taken now, so that the atomic's round trip overlaps
-    // the fence and barrier below.  (A CTA then holds two items; the lowest
-    // unfinished item is still always one being worked on, whose waits are
-    // for lower items only: no deadlock.)
-    unsigned long long nxt = 0;
-    if (threadIdx.x == 0) nxt = atomicAdd(Q.next, 1ULL);
     // Release: the CTA barrier orders every thread's writes before thread
     // 0's release reduction, which makes them visible before the count.
     __syncthreads();
@@ -236,11 +252,29 @@ struct BatchVariant {
   int rows, warps, depth, tile_h, tile_w;
   const void* kernel[3];  // by precision: FP32, mixed FP16, mixed BF16
   void (*launch[3])(int grid, const BQueue& q, cudaStream_t st);
+  void (*prepare[3])();   // shared-memory opt-in, once per device before the first launch
 };
+
+// Dynamic shared memory of a launch: the job records and tile entries when
+// they fit in kBatchSmemTables bytes, else none (read from global memory).
+constexpr size_t kBatchSmemTables = 160 * 1024;
+
+size_t batch_smem_bytes(int njobs, int ntiles) {
+  const size_t b = sizeof(BJobDev) * (size_t)njobs + sizeof(int2) * (size_t)ntiles;
+  return b <= kBatchSmemTables ? b : 0;
+}
 
 template <int R, int W, int K, typename TS>
 void launch_batch(int grid, const BQueue& q, cudaStream_t st) {
-  batch_persistent_kernel<R, W, K, TS><<<grid, W * 32, 0, st>>>(q);
+  const size_t dyn = q.smem_tables ? batch_smem_bytes(q.njobs, q.ntiles) : 0;
+  batch_persistent_kernel<R, W, K, TS><<<grid, W * 32, dyn, st>>>(q);
+}
+
+template <int R, int W, int K, typename TS>
+void prepare_batch() {
+  FPIE_CUDA(cudaFuncSetAttribute(batch_persistent_kernel<R, W, K, TS>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kBatchSmemTables));
 }
 
 template <int R, int W, int K>
@@ -250,7 +284,9 @@ BatchVariant make_bv(const char* name) {
                        (const void*)&batch_persistent_kernel<R, W, K, __half>,
                        (const void*)&batch_persistent_kernel<R, W, K, __nv_bfloat16>},
                       {&launch_batch<R, W, K, float>, &launch_batch<R, W, K, __half>,
-                       &launch_batch<R, W, K, __nv_bfloat16>}};
+                       &launch_batch<R, W, K, __nv_bfloat16>},
+                      {&prepare_batch<R, W, K, float>, &prepare_batch<R, W, K, __half>,
+                       &prepare_batch<R, W, K, __nv_bfloat16>}};
 }
 
 static const std::vector<BatchVariant>& batch_variants() {
@@ -437,26 +473,54 @@ struct Batch {
     return jobs[id];
   }
 
-  // (tile index, flag) of the active tiles of a job for a variant's tiling.
-  static void tile_list(const BatchJob& j, const BatchVariant& v, std::vector<int2>& out,
-                        int& tiles_x) {
-    tiles_x = (j.m + v.tile_w - 1) / v.tile_w;
-    const int tiles_y = (j.n + v.tile_h - 1) / v.tile_h;
-    out.clear();
-    for (int ty = 0; ty < tiles_y; ++ty)
-      for (int tx = 0; tx < tiles_x; ++tx) {
-        const int r0 = ty * v.tile_h, c0 = tx * v.tile_w;
-        bool any = false, all = true;
-        for (int i = r0 - v.depth; i < r0 + v.tile_h + v.depth; ++i)
-          for (int k = c0 - v.depth; k < c0 + v.tile_w + v.depth; ++k) {
-            const bool in = i >= 0 && i < j.n && k >= 0 && k < j.m;
-            const bool on = in && j.hmask[(size_t)i * j.m + k];
-            all = all && on;
-            if (on && i >= r0 && i < r0 + v.tile_h && k >= c0 && k < c0 + v.tile_w) any = true;
-          }
-        if (any) out.push_back(make_int2(ty * tiles_x + tx, all ? 2 : 1));
+  // (tile index, flag) of the active tiles of a job for every variant's
+  // tiling: a tile is active if a masked pixel lies in it, and fully masked
+  // (flag 2) if every pixel of its region (tile + depth on each side) lies
+  // in the crop and is masked.  Counted with one summed-area table of the
+  // mask, so each tile costs four lookups instead of a scan of its region.
+  static void tile_lists(BatchJob& j) {
+    const int n = j.n, m = j.m;
+    const size_t w = (size_t)m + 1;
+    std::vector<int> S((size_t)(n + 1) * w, 0);
+    for (int i = 0; i < n; ++i) {
+      int row = 0;
+      for (int k = 0; k < m; ++k) {
+        row += j.hmask[(size_t)i * m + k] ? 1 : 0;
+        S[(size_t)(i + 1) * w + k + 1] = S[(size_t)i * w + k + 1] + row;
       }
+    }
+    // Masked pixels in rows [r0, r1) x columns [c0, c1), clipped to the crop.
+    auto count = [&](int r0, int r1, int c0, int c1) -> long long {
+      r0 = std::max(r0, 0), c0 = std::max(c0, 0), r1 = std::min(r1, n), c1 = std::min(c1, m);
+      if (r0 >= r1 || c0 >= c1) return 0;
+      return (long long)S[(size_t)r1 * w + c1] - S[(size_t)r0 * w + c1] - S[(size_t)r1 * w + c0] +
+             S[(size_t)r0 * w + c0];
+    };
+    const auto& vs = batch_variants();
+    j.tiles_of.assign(vs.size(), {});
+    j.tiles_x_of.assign(vs.size(), -1);
+    for (size_t vi = 0; vi < vs.size(); ++vi) {
+      const BatchVariant& v = vs[vi];
+      const int tiles_x = (m + v.tile_w - 1) / v.tile_w;
+      const int tiles_y = (n + v.tile_h - 1) / v.tile_h;
+      std::vector<int2>& out = j.tiles_of[vi];
+      for (int ty = 0; ty < tiles_y; ++ty)
+        for (int tx = 0; tx < tiles_x; ++tx) {
+          const int r0 = ty * v.tile_h, c0 = tx * v.tile_w;
+          if (count(r0, r0 + v.tile_h, c0, c0 + v.tile_w) == 0) continue;
+          const int R0 = r0 - v.depth, R1 = r0 + v.tile_h + v.depth;
+          const int C0 = c0 - v.depth, C1 = c0 + v.tile_w + v.depth;
+          const bool inside = R0 >= 0 && C0 >= 0 && R1 <= n && C1 <= m;
+          const bool all = inside && count(R0, R1, C0, C1) == (long long)(R1 - R0) * (C1 - C0);
+          out.push_back(make_int2(ty * tiles_x + tx, all ? 2 : 1));
+        }
+      j.tiles_x_of[vi] = tiles_x;
+    }
   }
+
+  // Kernels whose dynamic shared-memory limit was raised (per variant and
+  // precision).
+  bool prepared[8][3] = {};
 
   // Runs `sweeps[id]` more sweeps of the listed jobs in one persistent launch
   // of variant v; returns the device milliseconds (measured with events).
@@ -467,11 +531,7 @@ struct Batch {
     std::vector<int> levels;
     for (size_t k = 0; k < ids.size(); ++k) {
       BatchJob& j = jobs[ids[k]];
-      if (j.tiles_of.size() != batch_variants().size()) {
-        j.tiles_of.assign(batch_variants().size(), {});
-        j.tiles_x_of.assign(batch_variants().size(), -1);
-      }
-      if (j.tiles_x_of[vi] < 0) tile_list(j, v, j.tiles_of[vi], j.tiles_x_of[vi]);
+      if (j.tiles_of.size() != batch_variants().size()) tile_lists(j);
       const std::vector<int2>& tl = j.tiles_of[vi];
       const int tx = j.tiles_x_of[vi];
       BJobDev d;
@@ -542,11 +602,18 @@ struct Batch {
       q.error = reinterpret_cast<int*>(dev + off + 8);
       q.nlevels = nlevels;
       q.njobs = nj;
+      q.ntiles = (int)tiles.size();
+      const size_t dyn = batch_smem_bytes(nj, (int)tiles.size());
+      q.smem_tables = dyn > 0 ? 1 : 0;
       q.spin_limit = spin_limit;
       FPIE_CUDA(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, stream));
+      if (!prepared[vi][precision]) {
+        v.prepare[precision]();
+        prepared[vi][precision] = true;
+      }
       int occ = 0;
       FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v.kernel[precision],
-                                                              v.warps * 32, 0));
+                                                              v.warps * 32, dyn));
       const int grid = std::max(1, occ) * sms;
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (time_it) {
