@@ -104,15 +104,19 @@ __device__ __forceinline__ void tbp_update(const float2 (&cur)[4], const float2 
   const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
                                 __shfl_down_sync(0xffffffffu, cur[0].y, 1));
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const float2 l = j > 0 ? cur[j - 1] : lf;
-    const float2 r = j < 3 ? cur[j + 1] : rt;
-    float2 t = __fadd2_rn(gv[j], up[j]);
-    t = __fadd2_rn(t, dn[j]);
-    t = __fadd2_rn(t, l);
-    t = __fadd2_rn(t, r);
-    o[j] = __fmul2_rn(t, q);
-  }
+  // The four column groups' chains advance together, one addition step at
+  // a time, so that independent packed adds sit next to each other.
+  float2 t[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(gv[j], up[j]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], dn[j]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], j > 0 ? cur[j - 1] : lf);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], j < 3 ? cur[j + 1] : rt);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) o[j] = __fmul2_rn(t[j], q);
   if (!FULL) {
     o[0] = pick2(mk[i], mk[i + H], 0x000000ffu, o[0], cur[0]);
     o[1] = pick2(mk[i], mk[i + H], 0x0000ff00u, o[1], cur[1]);
@@ -252,18 +256,28 @@ __device__ __forceinline__ void tbp_rb_half(float2 (&P)[R / 2][4], const float2 
                                             __shfl_up_sync(0xffffffffu, src.y, 1))
                               : make_float2(__shfl_down_sync(0xffffffffu, src.x, 1),
                                             __shfl_down_sync(0xffffffffu, src.y, 1));
+    float2 up[2], dn[2], l[2], r[2], t[2];
 #pragma unroll
     for (int jj = 0; jj < 2; ++jj) {
       const int j = j0 + 2 * jj;
-      const float2 up = i > 0 ? P[i - 1][j] : make_float2(av[j], P[H - 1][j].x);
-      const float2 dn = i < H - 1 ? P[i + 1][j] : make_float2(P[0][j].y, bv[j]);
-      const float2 l = j > 0 ? P[i][j - 1] : nb;
-      const float2 r = j < 3 ? P[i][j + 1] : nb;
-      float2 t = __fadd2_rn(Gp[i][j], up);
-      t = __fadd2_rn(t, dn);
-      t = __fadd2_rn(t, l);
-      t = __fadd2_rn(t, r);
-      const float2 o = __fmul2_rn(t, q);
+      up[jj] = i > 0 ? P[i - 1][j] : make_float2(av[j], P[H - 1][j].x);
+      dn[jj] = i < H - 1 ? P[i + 1][j] : make_float2(P[0][j].y, bv[j]);
+      l[jj] = j > 0 ? P[i][j - 1] : nb;
+      r[jj] = j < 3 ? P[i][j + 1] : nb;
+    }
+    // The two column groups' chains advance together, one step at a time.
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) t[jj] = __fadd2_rn(Gp[i][j0 + 2 * jj], up[jj]);
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) t[jj] = __fadd2_rn(t[jj], dn[jj]);
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) t[jj] = __fadd2_rn(t[jj], l[jj]);
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) t[jj] = __fadd2_rn(t[jj], r[jj]);
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) {
+      const int j = j0 + 2 * jj;
+      const float2 o = __fmul2_rn(t[jj], q);
       P[i][j] = FULL ? o : pick2(mk[i], mk[i + H], 0xffu << (8 * j), o, P[i][j]);
     }
   }
