@@ -797,13 +797,21 @@ struct GridSolverImpl : Solver {
         return 0;
       }
     }
-    // Candidates: the packed temporally blocked variants, then the flow
-    // kernel below.  sweep1, the scalar "r" variants and the TMA and
-    // resident kernels stay available by name but were never the fastest
-    // on any measured shape; timing them would only lengthen the first step.
+    // Candidates: three packed temporally blocked variants, then the flow
+    // kernel and (when it fits) the resident kernel below.  The other
+    // variants (sweep1, the scalar "r" ones, the shallower or shared-grad
+    // packed ones, the TMA kernel) stay available by name but were never the
+    // fastest on a measured shape; timing them would only lengthen the first
+    // step.
+    static const char* const kTuned[] = {"p16w8k16", "p8w16k16", "p16w8k8"};
     std::vector<int> cands;
-    for (int v = 0; v < (int)tb_variants().size(); ++v)
-      if (red_black ? tb_variants()[v].red_black : tb_variants()[v].name[0] == 'p') cands.push_back(v);
+    for (int v = 0; v < (int)tb_variants().size(); ++v) {
+      const TbVariant& tv = tb_variants()[v];
+      bool take = tv.red_black;
+      if (!red_black)
+        for (const char* n : kTuned) take = take || std::string(tv.name) == n;
+      if (take && tv.red_black == red_black) cands.push_back(v);
+    }
     const int ncand = (int)cands.size();
     if (iters < (ncand + 1) * (kTuneReps + 1) * kChunk + kChunk) return 0;
     cudaEvent_t e0, e1;
