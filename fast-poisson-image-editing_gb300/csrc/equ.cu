@@ -19,7 +19,7 @@ namespace fpie {
 void launch_prep_mask(const uint8_t* mask, int mh, int mw, int mch, uint8_t* m01, int* box,
                       cudaStream_t st);
 int launch_equ_ids(const uint8_t* m01, int mw, int x0, int y0, int n, int m, int* counts,
-                   int* ids, cudaStream_t st);
+                   int* ids, cudaStream_t st, bool red_black);
 void launch_equ_build(const uint8_t* m01, int mw, int x0, int y0, int n, int m, const int* ids,
                       const uint8_t* src, int sw, int sx, int sy, const uint8_t* tgt, int tw,
                       int tx, int ty, int mode, long long np, int4* A, float* xa, float* xb,
@@ -637,9 +637,6 @@ struct EquSolverImpl : Solver {
                    const uint8_t* tgt, int th, int tw, int s_row, int s_col, int t_row, int t_col,
                    int mode, bool on_device, int* box_out) {
     FPIE_REQUIRE(src && msk && tgt && box_out, FPIE_ERR_ARG, "null input array");
-    FPIE_REQUIRE(order == FPIE_ORDER_JACOBI, FPIE_ERR_STATE,
-                 "reset from images numbers unknowns row-major; red-black order needs "
-                 "partition() + reset()");
     FPIE_REQUIRE(sh > 0 && sw > 0 && mh > 0 && mw > 0 && th > 0 && tw > 0, FPIE_ERR_ARG, "empty image");
     FPIE_REQUIRE(mch == 1 || mch == 3, FPIE_ERR_ARG, "mask must have 1 or 3 channels");
     FPIE_REQUIRE(mode >= 0 && mode <= 2, FPIE_ERR_ARG, "gradient mode must be 0 (src), 1 (avg), 2 (max)");
@@ -678,11 +675,15 @@ struct EquSolverImpl : Solver {
     if (!fits)
       throw Error{FPIE_ERR_ARG, "the mask's crop at the given offsets leaves the source or target image"};
     const int n = x1 - x0, m = y1 - y0;
-    const int nb = launch_equ_ids(m01, mw, x0, y0, n, m, counts, ids, stream);
-    post_launch(this, 3);
-    int unknowns = 0;
-    FPIE_CUDA(cudaMemcpyAsync(&unknowns, counts + nb, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    const bool rb = order == FPIE_ORDER_RED_BLACK;
+    const int nb = launch_equ_ids(m01, mw, x0, y0, n, m, counts, ids, stream, rb);
+    post_launch(this, rb ? 7 : 3);
+    int tallies[2] = {0, 0};  // unknowns, and (red-black) the odd ones
+    FPIE_CUDA(cudaMemcpyAsync(tallies, counts + nb, (rb ? 2 : 1) * sizeof(int),
+                              cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
+    const int unknowns = tallies[0];
+    if (rb) n_mid = tallies[1] + 1;
     const int N = unknowns + 1;
     allocate(N);
     cudaFree(d_rows);

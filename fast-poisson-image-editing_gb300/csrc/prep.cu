@@ -122,7 +122,10 @@ void launch_prep_grid(const PrepArgs& a, uint8_t* mask, float* xa, float* xb, fl
 // ---- equation form ---------------------------------------------------------------
 // ids: 1-based row-major ranks of the set pixels of the crop (the reference's
 // partition + ids[mask == 0] = 0, fpie/process.py:281-291), by a three-step
-// scan over blocks of kScanTile pixels.
+// scan over blocks of kScanTile pixels.  Red-black numbering (the OpenMP
+// EquSolver's partition, fpie/core/openmp/equ.cc:22-56): the same scan over
+// the cells with odd row + col of the crop, then over the even ones, whose
+// ranks continue after the odd count.
 namespace fpie {
 
 constexpr int kScanTile = 1024;  // 256 threads x 4 pixels
@@ -130,8 +133,10 @@ constexpr int kScanTile = 1024;  // 256 threads x 4 pixels
 struct CropView {
   const uint8_t* m01;
   int mw, x0, y0, n, m;
+  int parity = -1;  // 0 / 1: only the cells with that parity of row + col count as set
   __device__ __forceinline__ int at(long long q) const {
     const int i = (int)(q / m), j = (int)(q % m);
+    if (parity >= 0 && ((i + j) & 1) != parity) return 0;
     return m01[(long long)(x0 + i) * mw + (y0 + j)];
   }
 };
@@ -179,8 +184,12 @@ __global__ void __launch_bounds__(1024) scan_offsets_kernel(int* __restrict__ co
   if (threadIdx.x == 0) counts[nb] = carry;
 }
 
+// base: added to every rank (NULL: 0); keep_others: leave the ids of cells
+// that do not count as set (second pass of the red-black numbering).
 __global__ void __launch_bounds__(256) scan_ids_kernel(CropView V, const int* __restrict__ offsets,
-                                                      int* __restrict__ ids) {
+                                                      int* __restrict__ ids,
+                                                      const int* __restrict__ base,
+                                                      bool keep_others) {
   const long long total = (long long)V.n * V.m;
   const long long start = (long long)blockIdx.x * kScanTile + threadIdx.x * 4;
   int on[4], c = 0;
@@ -202,11 +211,14 @@ __global__ void __launch_bounds__(256) scan_ids_kernel(CropView V, const int* __
   __syncthreads();
   int before = 0;
   for (int k = 0; k < w; ++k) before += warp_tot[k];
-  int rank = offsets[blockIdx.x] + before + incl - c;
+  int rank = (base ? *base : 0) + offsets[blockIdx.x] + before + incl - c;
 #pragma unroll
   for (int k = 0; k < 4; ++k)
-    if (start + k < total) ids[start + k] = on[k] ? ++rank : 0;
+    if (start + k < total && (on[k] || !keep_others)) ids[start + k] = on[k] ? ++rank : 0;
 }
+
+// counts[nb] = odd + even unknowns, counts[nb + 1] = odd ones.
+__global__ void rb_total_kernel(int* counts, int nb) { counts[nb] += counts[nb + 1]; }
 
 struct EquPrepArgs {
   CropView V;
@@ -268,13 +280,26 @@ __global__ void equ_build_kernel(EquPrepArgs P, int4* __restrict__ A, float* __r
 }
 
 int launch_equ_ids(const uint8_t* m01, int mw, int x0, int y0, int n, int m, int* counts,
-                   int* ids, cudaStream_t st) {
+                   int* ids, cudaStream_t st, bool red_black) {
   CropView V{m01, mw, x0, y0, n, m};
   const long long total = (long long)n * m;
   const int nb = (int)((total + kScanTile - 1) / kScanTile);
+  if (!red_black) {
+    scan_count_kernel<<<nb, 256, 0, st>>>(V, counts);
+    scan_offsets_kernel<<<1, 1024, 0, st>>>(counts, nb);
+    scan_ids_kernel<<<nb, 256, 0, st>>>(V, counts, ids, nullptr, false);
+    return nb;
+  }
+  V.parity = 1;  // odd cells: ids 1.., every other cell 0
   scan_count_kernel<<<nb, 256, 0, st>>>(V, counts);
   scan_offsets_kernel<<<1, 1024, 0, st>>>(counts, nb);
-  scan_ids_kernel<<<nb, 256, 0, st>>>(V, counts, ids);
+  scan_ids_kernel<<<nb, 256, 0, st>>>(V, counts, ids, nullptr, false);
+  FPIE_CUDA(cudaMemcpyAsync(counts + nb + 1, counts + nb, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  V.parity = 0;  // even cells: ids after the odd count
+  scan_count_kernel<<<nb, 256, 0, st>>>(V, counts);
+  scan_offsets_kernel<<<1, 1024, 0, st>>>(counts, nb);
+  scan_ids_kernel<<<nb, 256, 0, st>>>(V, counts, ids, counts + nb + 1, true);
+  rb_total_kernel<<<1, 1, 0, st>>>(counts, nb);
   return nb;
 }
 

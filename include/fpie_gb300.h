@@ -76,8 +76,8 @@ int fpie_equ_partition(fpie_solver* s, const int32_t* mask, int n, int m,
  * discards the loaded system: call partition and reset again.  In red-black
  * order reset checks that every unknown's neighbours have the other colour
  * for the last partition's n_mid (FPIE_ERR_ARG if not, FPIE_ERR_STATE if no
- * partition was made), the sweeps run on the equation kernels, and
- * fpie_equ_reset_images is refused (it numbers unknowns row-major). */
+ * partition was made), and fpie_equ_reset_images numbers the unknowns as
+ * the red-black partition does (n_mid from its own count). */
 int fpie_equ_set_order(fpie_solver* s, int order);
 
 /* The current order and, if n_mid is not NULL, the last red-black

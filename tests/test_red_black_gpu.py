@@ -197,23 +197,39 @@ def test_order_change_discards_the_system(backend):
     np.testing.assert_array_equal(ids[e["mask"] > 0], np.arange(1, int((e["mask"] > 0).sum()) + 1))
 
 
-def test_reset_images_refused(backend):
-    d = load_golden("rand24")
+@pytest.mark.parametrize("name", OMP_EQU_CASES)
+def test_reset_images_numbers_red_black(backend, name):
+    """The GPU-side reset from the uint8 images builds the red-black system:
+    the OpenMP partition's numbering, the host reset's A / B, and the same
+    sweeps."""
+    d = load_golden(name)
     src, mask, tgt, mos, mot, grad = problem_args(d)
+    e = oprep.equ_inputs(src, mask, tgt, mos, mot, grad, order="red_black")
     s = backend.EquSolver(1024, order="red_black")
-    with pytest.raises(RuntimeError, match="red-black"):
-        s.reset_images(src, mask, tgt, mos, mot, grad)
+    N, box, (rows, cols) = s.reset_images(src, mask, tgt, mos, mot, grad)
+    assert N == e["N"] and s.n_mid == e["n_mid"]
+    A, B = s.inputs()
+    np.testing.assert_array_equal(A, e["A"])
+    np.testing.assert_array_equal(B, e["B"])
+    np.testing.assert_array_equal(rows, e["tgt_index"][0])
+    np.testing.assert_array_equal(cols, e["tgt_index"][1])
+    s.step(37)
+    o = np_jacobi.EquRedBlack(e["A"], e["X"], e["B"], e["n_mid"])
+    o.sweep(37)
+    np.testing.assert_array_equal(s.state(), o.X)
 
 
 @pytest.mark.parametrize("name", ["circle256", "blob_frame"])
-def test_processor_matches_reference_openmp(name):
-    """EquProcessor(backend='gb300-rb') end to end equals the reference's
-    OpenMP EquProcessor's merged images (the golden crop)."""
+@pytest.mark.parametrize("device_prep", [False, True])
+def test_processor_matches_reference_openmp(name, device_prep):
+    """EquProcessor(backend='gb300-rb') end to end, host or GPU-side reset,
+    equals the reference's OpenMP EquProcessor's merged images (the golden
+    crop)."""
     from fpie_gb300 import process
 
     d = load_golden(name)
     src, mask, tgt, mos, mot, grad = problem_args(d)
-    p = process.EquProcessor(gradient=grad, backend="gb300-rb")
+    p = process.EquProcessor(gradient=grad, backend="gb300-rb", device_prep=device_prep)
     p.reset(src, mask, tgt, mos, mot)
     x0, x1, y0, y1 = (int(v) for v in d["grid_box"])
     done = 0
