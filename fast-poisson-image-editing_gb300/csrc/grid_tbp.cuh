@@ -103,7 +103,6 @@ __device__ __forceinline__ void tbp_update(const float2 (&cur)[4], const float2 
                                 __shfl_up_sync(0xffffffffu, cur[3].y, 1));
   const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
                                 __shfl_down_sync(0xffffffffu, cur[0].y, 1));
-#pragma unroll
   // The four column groups' chains advance together, one addition step at
   // a time, so that independent packed adds sit next to each other.
   float2 t[4];
