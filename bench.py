@@ -668,8 +668,11 @@ def run_gb300(args):
             line["error_vs_fp64"] = error_vs_fp64(check.state(), x64, mc, secs)
             origin = prep.grid_inputs(pb.src, pb.mask, pb.tgt, pb.mask_on_src, pb.mask_on_tgt,
                                       pb.gradient)[3]
-            line["reference_cuda"] = reference_cuda(mc, t, g, sysm if not args.no_equ else None, x64,
-                                                    (origin.x0, origin.y0))
+            try:
+                line["reference_cuda"] = reference_cuda(mc, t, g, sysm if not args.no_equ else None,
+                                                        x64, (origin.x0, origin.y0))
+            except Exception as exc:  # the comparison arm must not cost the bench line
+                line["reference_cuda"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
