@@ -607,6 +607,8 @@ struct Batch {
       q.smem_tables = dyn > 0 ? 1 : 0;
       q.spin_limit = spin_limit;
       FPIE_CUDA(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, stream));
+      FPIE_REQUIRE(vi >= 0 && vi < 8 && precision >= 0 && precision < 3, FPIE_ERR_STATE,
+                   "batch kernel variant out of range");
       if (!prepared[vi][precision]) {
         v.prepare[precision]();
         prepared[vi][precision] = true;
