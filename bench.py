@@ -743,6 +743,17 @@ def run_batch(args):
             "sequential_gridsolver": {"value": work / seq_s, "seconds": seq_s},
             "batched_seconds": batch_s, "speedup_vs_sequential": seq_s / batch_s,
             "gpu_launches": launches, "parity_spot_check": same, "parity_max_abs_diff": worst}
+    # Algorithmic bytes of the whole run: 37 B per crop pixel per sweep (FP32;
+    # the mixed forms' inner sweeps move 25 B) over every job's sweeps.
+    per_px = GRID_BYTES_PER_PX if args.precision == "fp32" else 25
+    alg = sum(per_px * mc.size * it for mc, t, g, it in jobs)
+    peak, peak_kind = measured_peak()
+    line["roofline"] = {"bound": "hbm", "achieved": alg / batch_s / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": alg / batch_s / 1e9 / peak, "traffic": None,
+                        "peak_source": peak_kind,
+                        "note": f"{per_px} B per crop pixel per sweep over all jobs' sweeps, "
+                                "divided by the batched wall time (autotuning included); above 1 "
+                                "because each pass keeps a region in registers for 16 sweeps"}
     print(json.dumps(line), flush=True)
 
 
