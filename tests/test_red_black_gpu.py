@@ -238,3 +238,14 @@ def test_processor_matches_reference_openmp(name, device_prep):
         done = k
         np.testing.assert_array_equal(img[x0:x1, y0:y1], d[f"omp_equ_img_{k}"])
         np.testing.assert_allclose(err, d[f"omp_equ_err_{k}"], rtol=1e-5, atol=1e-2)
+
+
+def test_order_arguments_checked(backend):
+    from fpie_gb300 import _abi
+
+    s = backend.EquSolver(256)
+    with pytest.raises(ValueError):
+        s.set_order("gauss")
+    with pytest.raises(_abi.FpieArgumentError):
+        _abi.call("fpie_equ_set_order", s._h, 7)
+    assert s.order == "jacobi" and s.n_mid == 0
