@@ -91,8 +91,8 @@ def test_cli_missing_source_exits_1(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method", ["grid", "equ"])
-def test_cli_end_to_end(tmp_path, method, monkeypatch):
+@pytest.mark.parametrize("method,backend", [("grid", "gb300"), ("equ", "gb300"), ("equ", "gb300-rb")])
+def test_cli_end_to_end(tmp_path, method, backend, monkeypatch):
     from fpie_gb300 import cli, workloads
     from fpie_gb300.process import EquProcessor, GridProcessor
 
@@ -101,11 +101,11 @@ def test_cli_end_to_end(tmp_path, method, monkeypatch):
         io.write_image(str(tmp_path / name), arr)
     monkeypatch.chdir(tmp_path)
     cli.main(["-s", "s.png", "-m", "m.png", "-t", "t.png", "-o", "o.png", "-n", "300", "-p", "100",
-              "-g", "src", "--method", method])
+              "-g", "src", "--method", method, "-b", backend])
     out = io.read_image(str(tmp_path / "o.png"))
     assert (tmp_path / "iter00100.png").exists() and (tmp_path / "iter00200.png").exists()
     mask3 = np.repeat(pb.mask[..., None], 3, -1)  # PNG round trip of a gray mask gives 3 channels
-    proc = (GridProcessor if method == "grid" else EquProcessor)(gradient="src", backend="gb300")
+    proc = (GridProcessor if method == "grid" else EquProcessor)(gradient="src", backend=backend)
     proc.reset(pb.src, mask3, pb.tgt, (0, 0), (0, 0))
     ref, _ = proc.step(300)
     np.testing.assert_array_equal(out, ref)
