@@ -40,6 +40,7 @@ _PROTOS: dict[str, tuple] = {
     "fpie_equ_create": ([_I, ctypes.POINTER(_P)], _I),
     "fpie_equ_partition": ([_P, _P, _I, _I, _P], _I),
     "fpie_equ_set_order": ([_P, _I], _I),
+    "fpie_equ_reset_placed": ([_P, _I, _P, _P, _P, _P, _I, _I], _I),
     "fpie_equ_order": ([_P, _P, _P], _I),
     "fpie_equ_reset": ([_P, _I, _P, _P, _P], _I),
     "fpie_equ_step": ([_P, _I, _P, _P], _I),

@@ -182,12 +182,22 @@ class EquSolver(_Solver):
         _abi.call("fpie_equ_partition", self._h, _ptr(m), m.shape[0], m.shape[1], _ptr(ids))
         return ids
 
-    def reset(self, N: int, A: np.ndarray, X: np.ndarray, B: np.ndarray) -> None:
+    def reset(self, N: int, A: np.ndarray, X: np.ndarray, B: np.ndarray,
+              placement: tuple[np.ndarray, int, int] | None = None) -> None:
+        """placement: optional (pos int32[N], n, m), unknown i at crop pixel
+        pos[i] = row * m + col -- checked on the device instead of searched
+        for on the host (fpie_equ_reset_placed)."""
         N = int(N)
         A = _as(A, np.int32, (N, 4), "A")
         X = _as(X, np.float32, (N, 3), "X")
         B = _as(B, np.float32, (N, 3), "B")
-        _abi.call("fpie_equ_reset", self._h, N, _ptr(A), _ptr(X), _ptr(B))
+        if placement is None:
+            _abi.call("fpie_equ_reset", self._h, N, _ptr(A), _ptr(X), _ptr(B))
+        else:
+            pos, n, m = placement
+            pos = _as(pos, np.int32, (N,), "pos")
+            _abi.call("fpie_equ_reset_placed", self._h, N, _ptr(A), _ptr(X), _ptr(B), _ptr(pos),
+                      int(n), int(m))
         self.N = N
 
     def step(self, iteration: int) -> tuple[np.ndarray, np.ndarray]:

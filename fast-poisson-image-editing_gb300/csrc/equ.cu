@@ -293,6 +293,22 @@ __global__ void equ_layout_check_kernel(EquGeom E, const int4* __restrict__ A,
   if (nbad) atomicAdd(bad, nbad);
 }
 
+// A caller's placement: counts unknowns that do not own their pixel (two on
+// one pixel) and, with a colouring (n_mid > 0), unknowns whose pixel has the
+// wrong parity of row + col (1..n_mid-1 odd, the others even).
+__global__ void equ_place_check_kernel(int N, const int* __restrict__ pos,
+                                       const int* __restrict__ occ, int m, int n_mid,
+                                       unsigned int* __restrict__ bad) {
+  unsigned int nbad = 0;
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int p = pos[i];
+    nbad += occ[p] != (int)i;
+    if (n_mid > 0) nbad += (((p / m + p % m) & 1) != 0) != (i < n_mid);
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
 __global__ void equ_occ_kernel(int N, const int* __restrict__ pos, int* __restrict__ occ) {
   for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
        i += (long long)gridDim.x * blockDim.x)
@@ -340,6 +356,7 @@ struct EquSolverImpl : Solver {
   int* d_occ = nullptr;             // unknown id per crop pixel
   int lay_N = 0, lay_n = 0, lay_m = 0;
   int lay_mid = 0;                  // the colouring it was placed for (0: none)
+  size_t occ_cap = 0;               // ints allocated at d_occ
   long long spin_limit = 1LL << 26;
 
   explicit EquSolverImpl(int block_size) {
@@ -527,8 +544,10 @@ struct EquSolverImpl : Solver {
                               stream));
     cudaFree(d_occ);
     d_occ = nullptr;
+    occ_cap = 0;
     lay_N = 0;
     FPIE_CUDA(cudaMalloc(&d_occ, sizeof(int) * (size_t)n * m));
+    occ_cap = (size_t)n * m;
     FPIE_CUDA(cudaMemsetAsync(d_occ, 0, sizeof(int) * (size_t)n * m, stream));
     equ_occ_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E.N, d_pos, d_occ);
     post_launch(this);
@@ -538,6 +557,76 @@ struct EquSolverImpl : Solver {
     lay_mid = colour_mid();
     enter_grid(n, m);
     FPIE_CUDA(cudaStreamSynchronize(stream));  // pos is a host vector
+  }
+
+  // After a reset with the caller's placement of the unknowns (pos[i] =
+  // row * m + col in an n x m crop, as EquProcessor knows it): the placement
+  // is checked on the device (every unknown alone on its pixel, its four
+  // grid neighbours exactly its A entries, row 0 the zero constant, and in
+  // red-black order the colour parity) instead of being searched for on the
+  // host.  A placement that does not fit the system is an argument error.
+  void choose_mode_placed(const int32_t* hpos, int n, int m) {
+    use_grid = false;
+    if (order == FPIE_ORDER_RED_BLACK) {
+      FPIE_REQUIRE(kernel_req == "auto" || kernel_req == "gather" || kernel_req.rfind("rb", 0) == 0,
+                   FPIE_ERR_ARG,
+                   "red-black order runs on its own kernels, not grid kernel '" + kernel_req + "'");
+      check_colouring();
+    }
+    if (kernel_req == "gather" || E.N < 2) return;
+    FPIE_REQUIRE(n >= 3 && m >= 3 && (long long)n * m <= (1LL << 31) / 4, FPIE_ERR_ARG,
+                 "placement crop must be at least 3 x 3 and below 2^29 pixels");
+    for (int i = 1; i < E.N; ++i) {  // interior pixels only: the check reads all four neighbours
+      const int p = hpos[i], r = p / m, c = p % m;
+      FPIE_REQUIRE(p >= 0 && r >= 1 && r <= n - 2 && c >= 1 && c <= m - 2, FPIE_ERR_ARG,
+                   "placement of unknown " + std::to_string(i) + " is not inside the crop's frame");
+    }
+    ensure_pos(E.N);
+    FPIE_CUDA(cudaMemcpyAsync(d_pos, hpos, sizeof(int) * (size_t)E.N, cudaMemcpyHostToDevice, stream));
+    lay_N = 0;
+    if (!d_occ || occ_cap < (size_t)n * m) {
+      cudaFree(d_occ);
+      d_occ = nullptr;
+      occ_cap = 0;
+      FPIE_CUDA(cudaMalloc(&d_occ, sizeof(int) * (size_t)n * m));
+      occ_cap = (size_t)n * m;
+    }
+    FPIE_CUDA(cudaMemsetAsync(d_occ, 0, sizeof(int) * (size_t)n * m, stream));
+    equ_occ_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E.N, d_pos, d_occ);
+    post_launch(this);
+    FPIE_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), stream));
+    equ_place_check_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E.N, d_pos, d_occ, m, colour_mid(),
+                                                                 d_bad);
+    post_launch(this);
+    equ_layout_check_kernel<<<conv_blocks(E.N), 256, 0, stream>>>(E, A, x[0], b, d_pos, d_occ, m,
+                                                                   d_bad);
+    post_launch(this);
+    FPIE_CUDA(cudaMemcpyAsync(h_bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    if (*h_bad) {
+      release();
+      throw Error{FPIE_ERR_ARG, "the placement does not fit the system: " + std::to_string(*h_bad) +
+                                    " mismatched unknowns or neighbours"};
+    }
+    lay_N = E.N;
+    lay_n = n;
+    lay_m = m;
+    lay_mid = colour_mid();
+    enter_grid(n, m);
+  }
+
+  void reset_host_placed(int N, const int32_t* hA, const float* hX, const float* hB,
+                         const int32_t* hpos, int n, int m) {
+    FPIE_REQUIRE(hA && hX && hB && hpos, FPIE_ERR_ARG, "null input array");
+    allocate(N);
+    AsyncScratch scratch((size_t)N * 24, stream);
+    float* stage = reinterpret_cast<float*>(scratch.bytes());
+    FPIE_CUDA(cudaMemcpyAsync(A, hA, (size_t)N * 16, cudaMemcpyHostToDevice, stream));
+    FPIE_CUDA(cudaMemcpyAsync(stage, hX, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+    FPIE_CUDA(cudaMemcpyAsync(stage + (size_t)N * 3, hB, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+    pack_and_check(stage, stage + (size_t)N * 3);
+    choose_mode_placed(hpos, n, m);
+    FPIE_CUDA(cudaStreamSynchronize(stream));
   }
 
   // x[cur] up to date with the grid state.
@@ -900,6 +989,11 @@ int fpie_equ_order(fpie_solver* s, int* order, int* n_mid) {
 int fpie_equ_reset(fpie_solver* s, int N, const int32_t* A, const float* X,
                    const float* B) {
   return guarded([&] { equ_of(s)->reset_host(N, A, X, B); });
+}
+
+int fpie_equ_reset_placed(fpie_solver* s, int N, const int32_t* A, const float* X, const float* B,
+                          const int32_t* pos, int n, int m) {
+  return guarded([&] { equ_of(s)->reset_host_placed(N, A, X, B, pos, n, m); });
 }
 
 int fpie_equ_step(fpie_solver* s, int iteration, uint8_t* x_out, float* err_out) {

@@ -110,6 +110,17 @@ class EquSystem:
     X: np.ndarray
     B: np.ndarray
     tgt_index: tuple[np.ndarray, np.ndarray]
+    crop: Crop | None = None  # the crop on the target
+
+    def placement(self) -> tuple[np.ndarray, int, int] | None:
+        """(pos int32[N], n, m): unknown i at row * m + col of the crop
+        (pos[0] = 0, unused), for EquSolver.reset(..., placement=...)."""
+        if self.crop is None:
+            return None
+        n, m = self.crop.x1 - self.crop.x0, self.crop.y1 - self.crop.y0
+        pos = np.zeros(self.N, np.int32)
+        pos[1:] = (self.tgt_index[0] - self.crop.x0) * m + (self.tgt_index[1] - self.crop.y0)
+        return pos, n, m
 
 
 def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) -> EquSystem:
@@ -144,4 +155,6 @@ def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) ->
     for dx, dy in ((-1, 0), (0, -1), (0, 1), (1, 0)):  # U, L, R, D
         outside = mc[px + dx, py + dy] == 0
         B[1:][outside] += tgt[tx + dx, ty + dy][outside].astype(np.float32)
-    return EquSystem(N, A, X, B, (tx, ty))
+    crop = Crop(mask_on_tgt[0] + cr.x0, mask_on_tgt[0] + cr.x1, mask_on_tgt[1] + cr.y0,
+                mask_on_tgt[1] + cr.y1)
+    return EquSystem(N, A, X, B, (tx, ty), crop)

@@ -130,7 +130,9 @@ class EquProcessor(BaseProcessor):
                                  self.core.partition)
         self.tgt = tgt.copy()
         self.tgt_index = system.tgt_index
-        self.core.reset(system.N, system.A, system.X, system.B)
+        # The mask gives every unknown's pixel: the solver checks that
+        # placement on the device instead of searching for one.
+        self.core.reset(system.N, system.A, system.X, system.B, placement=system.placement())
         return system.N
 
     def step(self, iteration: int):

@@ -90,6 +90,17 @@ int fpie_equ_order(fpie_solver* s, int* order, int* n_mid);
 int fpie_equ_reset(fpie_solver* s, int N, const int32_t* A, const float* X,
                    const float* B);
 
+/* fpie_equ_reset with the caller's placement of the unknowns on a grid:
+ * pos int32[N] (pos[0] ignored) = row * m + col of unknown i in an n x m
+ * crop, every unknown off the crop's 1-pixel frame -- what EquProcessor
+ * knows from its mask (fpie/process.py:321-372).  The placement is checked
+ * on the device (each unknown alone on its pixel, its four grid neighbours
+ * exactly its A entries, row 0 the zero constant, in red-black order the
+ * colour parity) instead of being searched for on the host; FPIE_ERR_ARG if
+ * it does not fit.  Results are those of fpie_equ_reset. */
+int fpie_equ_reset_placed(fpie_solver* s, int N, const int32_t* A, const float* X,
+                          const float* B, const int32_t* pos, int n, int m);
+
 /* Replaces EquSolver.step (fpie/core/cuda/equ.cu:189-211,
  * fpie/core/openmp/equ.cc:107-125): runs `iteration` sweeps (Jacobi, or
  * red-black in that order) continuing from the current state, then writes

@@ -9,7 +9,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import load_golden, problem_args
 from oracle import cjacobi
 
 pytestmark = pytest.mark.gpu
@@ -187,3 +187,44 @@ def test_grid_placement_from_images(backend):
     xq, eq = q.step(300)
     np.testing.assert_array_equal(xs, xq)
     np.testing.assert_array_equal(s.state(), q.state())
+
+
+def test_placed_reset_equals_the_searched_placement(backend, golden):
+    """reset with the processor's placement (checked on the device) runs the
+    same grid sweeps as reset without it (placement searched on the host)."""
+    from fpie_gb300 import prep as pprep
+
+    name, d = golden
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    a = backend.EquSolver(1024)
+    sysm = pprep.equ_inputs(src, mask, tgt, mos, mot, grad, a.partition)
+    a.reset(sysm.N, sysm.A, sysm.X, sysm.B, placement=sysm.placement())
+    b = backend.EquSolver(1024)
+    b.reset(sysm.N, sysm.A, sysm.X, sysm.B)
+    assert a.kernel.startswith("grid:") and a.kernel == b.kernel
+    for k in (5, 70):
+        xa, ea = a.step(k)
+        xb, eb = b.step(k)
+        np.testing.assert_array_equal(a.state(), b.state())
+        np.testing.assert_array_equal(xa, xb)
+        np.testing.assert_array_equal(ea, eb)
+
+
+def test_wrong_placement_is_refused(backend):
+    from fpie_gb300 import prep as pprep
+
+    d = load_golden("circle256")
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    s = backend.EquSolver(1024)
+    sysm = pprep.equ_inputs(src, mask, tgt, mos, mot, grad, s.partition)
+    pos, n, m = sysm.placement()
+    bad = pos.copy()
+    bad[1], bad[2] = pos[2], pos[1]  # two unknowns swapped
+    with pytest.raises(ValueError):
+        s.reset(sysm.N, sysm.A, sysm.X, sysm.B, placement=(bad, n, m))
+    edge = pos.copy()
+    edge[1] = 0  # on the crop's frame
+    with pytest.raises(ValueError):
+        s.reset(sysm.N, sysm.A, sysm.X, sysm.B, placement=(edge, n, m))
+    s.reset(sysm.N, sysm.A, sysm.X, sysm.B, placement=(pos, n, m))  # and the right one works
+    assert s.kernel.startswith("grid:")

@@ -100,3 +100,20 @@ def test_no_gpu_means_a_loud_error():
         backend.GridSolver(8, 8)
     with pytest.raises(_abi.FpieError):
         backend.EquSolver(256)
+
+
+def test_equ_placement_follows_the_target_index(golden):
+    from fpie_gb300 import prep as pprep
+    from oracle import np_jacobi
+
+    name, d = golden
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    for part in (lambda mc: np.cumsum((mc > 0).reshape(-1)).reshape(mc.shape),
+                 lambda mc: np_jacobi.red_black_ids(mc)[0]):
+        sysm = pprep.equ_inputs(src, mask, tgt, mos, mot, grad, part)
+        pos, n, m = sysm.placement()
+        assert (n, m) == tuple(d["grid_mask"].shape)
+        r, c = pos[1:] // m, pos[1:] % m
+        np.testing.assert_array_equal(r + sysm.crop.x0, sysm.tgt_index[0])
+        np.testing.assert_array_equal(c + sysm.crop.y0, sysm.tgt_index[1])
+        assert (d["grid_mask"][r, c] != 0).all()

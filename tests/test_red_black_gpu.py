@@ -249,3 +249,34 @@ def test_order_arguments_checked(backend):
     with pytest.raises(_abi.FpieArgumentError):
         _abi.call("fpie_equ_set_order", s._h, 7)
     assert s.order == "jacobi" and s.n_mid == 0
+
+
+def test_placed_reset_in_red_black_order(backend):
+    from fpie_gb300 import prep as pprep
+
+    d = load_golden("blob_frame")
+    src, mask, tgt, mos, mot, grad = problem_args(d)
+    s = backend.EquSolver(1024, order="red_black")
+    sysm = pprep.equ_inputs(src, mask, tgt, mos, mot, grad, s.partition)
+    s.reset(sysm.N, sysm.A, sysm.X, sysm.B, placement=sysm.placement())
+    assert s.kernel == "grid:rb16w8k8"
+    s.step(33)
+    o = np_jacobi.EquRedBlack(sysm.A, sysm.X, sysm.B, s.n_mid)
+    o.sweep(33)
+    np.testing.assert_array_equal(s.state(), o.X)
+    # the colours must sit on their parity: a placement shifted by one column is refused
+    pos, n, m = sysm.placement()
+    shifted = pos.copy()
+    shifted[1:] = (pos[1:] // m) * (m + 1) + pos[1:] % m + 1  # one column right: parity flips
+    t = backend.EquSolver(1024, order="red_black")
+    t.partition(d["grid_mask"])
+    with pytest.raises(ValueError):
+        t.reset(sysm.N, sysm.A, sysm.X, sysm.B, placement=(shifted, n, m + 1))
+    # the same shift is a valid placement for the Jacobi order (no colouring)
+    j = backend.EquSolver(1024)
+    jsys = pprep.equ_inputs(src, mask, tgt, mos, mot, grad, j.partition)
+    jpos, jn, jm = jsys.placement()
+    jshift = jpos.copy()
+    jshift[1:] = (jpos[1:] // jm) * (jm + 1) + jpos[1:] % jm + 1
+    j.reset(jsys.N, jsys.A, jsys.X, jsys.B, placement=(jshift, jn, jm + 1))
+    assert j.kernel.startswith("grid:")
