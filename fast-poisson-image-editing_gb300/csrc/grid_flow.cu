@@ -26,6 +26,12 @@
 // wave tail -- when a level has, say, 243 items on 152 SMs, CTAs that are
 // done with their level-z items go on to level z + 1 items whose
 // neighbourhoods are ready instead of idling until the whole level ends.
+//
+// The same launch runs the mixed forms (TS = __half / __nv_bfloat16: the
+// refinement cycles' level schedule) and, for the EquSolver's red-black
+// order on its grid placement ("rb16w8k8d"), levels of 8 red-black sweeps on
+// the same tiles and apron (16 half-steps, each shrinking the valid region
+// by one cell).
 #include <algorithm>
 #include <atomic>
 #include <type_traits>
