@@ -62,11 +62,8 @@ def mix(a: np.ndarray, b: np.ndarray, gradient: str) -> np.ndarray:
         return a
     if gradient == "avg":
         return (a + b) / 2
-    if gradient == "max":
-        take_b = np.abs(a) < np.abs(b)
-        a = a.copy()
-        a[take_b] = b[take_b]
-        return a
+    if gradient == "max":  # b where |a| < |b|, else a (a select: no arithmetic)
+        return np.where(np.abs(a) < np.abs(b), b, a)
     raise ValueError(f"unknown gradient mode {gradient!r}")
 
 
@@ -124,7 +121,15 @@ class EquSystem:
 
 
 def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) -> EquSystem:
-    """Build A/X/B; ``partition`` is the solver's id assignment (mask -> ids)."""
+    """Build A/X/B; ``partition`` is the solver's id assignment (mask -> ids).
+
+    The arithmetic is the reference's, per unknown and in its order
+    (fpie/process.py:321-372): the gradient sums the mixed L, R, U, D terms,
+    B then adds the target value of each unmasked neighbour in U, L, R, D
+    order.  It runs on whole slabs of the crop (every unknown lies inside
+    the crop's 1-pixel frame) and gathers the unknowns' rows once, instead
+    of gathering neighbour by neighbour.
+    """
     m01 = binary_mask(mask)
     cr = bounding_crop(m01)
     _check_offsets(mask.shape[:2], src.shape, mask_on_src, cr, "source")
@@ -133,28 +138,37 @@ def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) ->
     ids = np.asarray(partition(mc)).astype(np.int64)
     ids[mc == 0] = 0
     px, py = np.nonzero(mc)
-    order = np.argsort(ids[px, py], kind="stable")
-    px, py = px[order], py[order]
+    key = ids[px, py]
+    if key.size and not (np.diff(key) > 0).all():  # row-major ids are already in order
+        order = np.argsort(key, kind="stable")
+        px, py = px[order], py[order]
     N = px.size + 1
-    sx, sy = px + mask_on_src[0] + cr.x0, py + mask_on_src[1] + cr.y0
-    tx, ty = px + mask_on_tgt[0] + cr.x0, py + mask_on_tgt[1] + cr.y0
-    sc = src[sx, sy].astype(np.float32)
-    tc = tgt[tx, ty].astype(np.float32)
+    sr, sc_ = mask_on_src[0] + cr.x0, mask_on_src[1] + cr.y0
+    tr, tc_ = mask_on_tgt[0] + cr.x0, mask_on_tgt[1] + cr.y0
+    n, m = mc.shape
+    s = src[sr:sr + n, sc_:sc_ + m].astype(np.float32)
+    t = tgt[tr:tr + n, tc_:tc_ + m].astype(np.float32)
+    # Interior [1:-1, 1:-1] of the crop and its four shifted neighbours.
+    inner = (slice(1, n - 1), slice(1, m - 1))
+    shifts = {"L": (slice(1, n - 1), slice(0, m - 2)), "R": (slice(1, n - 1), slice(2, m)),
+              "U": (slice(0, n - 2), slice(1, m - 1)), "D": (slice(2, n), slice(1, m - 1))}
+    s0, t0 = s[inner], t[inner]
     grad = None
-    for dx, dy in ((0, -1), (0, 1), (-1, 0), (1, 0)):  # L, R, U, D
-        term = mix(sc - src[sx + dx, sy + dy].astype(np.float32),
-                   tc - tgt[tx + dx, ty + dy].astype(np.float32), gradient)
+    for d in ("L", "R", "U", "D"):
+        term = mix(s0 - s[shifts[d]], t0 - t[shifts[d]], gradient)
         grad = term if grad is None else grad + term
+    bsum = grad
+    for d in ("U", "L", "R", "D"):
+        outside = np.broadcast_to((mc[shifts[d]] == 0)[..., None], bsum.shape)
+        np.add(bsum, t[shifts[d]], out=bsum, where=outside)
+    q = (px - 1) * (m - 2) + (py - 1)  # unknowns as flat indices of the interior
     A = np.zeros((N, 4), np.int32)
     X = np.zeros((N, 3), np.float32)
     B = np.zeros((N, 3), np.float32)
-    X[1:] = tc
-    for k, (dx, dy) in enumerate(((-1, 0), (1, 0), (0, -1), (0, 1))):  # U, D, L, R
-        A[1:, k] = ids[px + dx, py + dy]
-    B[1:] = grad
-    for dx, dy in ((-1, 0), (0, -1), (0, 1), (1, 0)):  # U, L, R, D
-        outside = mc[px + dx, py + dy] == 0
-        B[1:][outside] += tgt[tx + dx, ty + dy][outside].astype(np.float32)
+    X[1:] = np.ascontiguousarray(t0).reshape(-1, 3)[q]
+    for k, d in enumerate(("U", "D", "L", "R")):
+        A[1:, k] = np.ascontiguousarray(ids[shifts[d]]).reshape(-1)[q]
+    B[1:] = bsum.reshape(-1, 3)[q]
     crop = Crop(mask_on_tgt[0] + cr.x0, mask_on_tgt[0] + cr.x1, mask_on_tgt[1] + cr.y0,
                 mask_on_tgt[1] + cr.y1)
-    return EquSystem(N, A, X, B, (tx, ty), crop)
+    return EquSystem(N, A, X, B, (px + tr, py + tc_), crop)

@@ -88,3 +88,18 @@ def test_red_black_sweep_is_a_gauss_seidel_sweep(p):
             s = s + X[a[3]]
             X[i] = s / np.float32(4.0)
     np.testing.assert_array_equal(o.X, X)
+
+
+@settings(max_examples=40, deadline=None)
+@given(problems(), st.sampled_from(["row", "red_black"]))
+def test_equ_inputs_match_the_oracle(p, order):
+    """The package's slab-based construction of A / X / B equals the oracle's
+    unknown-by-unknown restatement, for either numbering."""
+    src, mask, tgt, mode = p
+    part = ((lambda mc: np.cumsum((mc > 0).reshape(-1)).reshape(mc.shape)) if order == "row"
+            else (lambda mc: np_jacobi.red_black_ids(mc)[0]))
+    e = oprep.equ_inputs(src, mask, tgt, (0, 0), (0, 0), mode, order=order)
+    s = prep.equ_inputs(src, mask, tgt, (0, 0), (0, 0), mode, part)
+    for k in ("A", "X", "B"):
+        np.testing.assert_array_equal(e[k], getattr(s, k))
+    np.testing.assert_array_equal(np.stack(e["tgt_index"]), np.stack(s.tgt_index))
