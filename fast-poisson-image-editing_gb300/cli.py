@@ -7,7 +7,7 @@ Same flags and prints as the reference; ``--check-backend`` lists
 ``ALL_BACKEND`` (the gb300 backends) and exits.  ``-p P`` writes
 ``iterNNNNN.png`` every P sweeps, as the reference does.  The solver inputs
 are built on the GPU from the uint8 images (bit-identical to the host
-construction, which takes 0.2-0.5 s with numpy on a 1024^2 target);
+construction, which takes 0.1-0.2 s with numpy on a 1024^2 target);
 ``--host-prep`` builds them on the host as the reference does.
 """
 
