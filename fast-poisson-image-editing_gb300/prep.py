@@ -11,8 +11,9 @@ bit for bit:
   fpie/process.py:214-223), with ties in 'max' keeping the source term;
 * grid inputs: grad = mixed(C-U) + mixed(C-D) + mixed(C-L) + mixed(C-R)
   summed in that order, zero outside the mask (fpie/process.py:455-479);
-* equation inputs: ids in row-major order, A = ids of (up, down, left,
-  right), grad summed (L, R, U, D), B = grad + target values of unmasked
+* equation inputs: ids from the solver's partition (row-major, or odd
+  cells first in red-black order), A = ids of (up, down, left, right),
+  grad summed (L, R, U, D), B = grad + target values of unmasked
   neighbours added (U, L, R, D), row 0 the constant 0 (fpie/process.py:
   281-372).
 """
