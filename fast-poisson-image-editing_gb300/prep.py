@@ -68,6 +68,25 @@ def mix(a: np.ndarray, b: np.ndarray, gradient: str) -> np.ndarray:
     raise ValueError(f"unknown gradient mode {gradient!r}")
 
 
+def _mixed_int(a: np.ndarray, b: np.ndarray, gradient: str) -> np.ndarray:
+    """mix() of integer differences of uint8 pixels, times _scale(gradient):
+    every mixed term is then an integer (|term| <= 510), so sums of up to
+    eight of them are exact in int16 -- and equal, after the division by the
+    scale, to the float32 results of mix(), whose partial sums (integers or
+    halves below 2^11) are exact as well."""
+    if gradient == "src":
+        return a
+    if gradient == "avg":
+        return a + b
+    if gradient == "max":
+        return np.where(np.abs(a) < np.abs(b), b, a)
+    raise ValueError(f"unknown gradient mode {gradient!r}")
+
+
+def _scale(gradient: str) -> int:
+    return 2 if gradient == "avg" else 1
+
+
 def _check_offsets(shape, img_shape, off, crop: Crop, name: str) -> None:
     if (off[0] + crop.x0 < 0 or off[1] + crop.y0 < 0
             or off[0] + crop.x1 > img_shape[0] or off[1] + crop.y1 > img_shape[1]):
@@ -84,18 +103,24 @@ def grid_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient):
     _check_offsets(mask.shape[:2], tgt.shape, mask_on_tgt, cr, "target")
     mc = m01[cr.x0:cr.x1, cr.y0:cr.y1]
     s = src[mask_on_src[0] + cr.x0:mask_on_src[0] + cr.x1,
-            mask_on_src[1] + cr.y0:mask_on_src[1] + cr.y1].astype(np.float32)
-    t = tgt[mask_on_tgt[0] + cr.x0:mask_on_tgt[0] + cr.x1,
-            mask_on_tgt[1] + cr.y0:mask_on_tgt[1] + cr.y1].astype(np.float32)
-    grad = np.zeros(t.shape, np.float32)
+            mask_on_src[1] + cr.y0:mask_on_src[1] + cr.y1].astype(np.int16)
+    ti = tgt[mask_on_tgt[0] + cr.x0:mask_on_tgt[0] + cr.x1,
+             mask_on_tgt[1] + cr.y0:mask_on_tgt[1] + cr.y1].astype(np.int16)
+    t = ti.astype(np.float32)
+    # Integer terms (see _mixed_int): the same values as the float32
+    # arithmetic of the reference, computed without rounding.
+    acc = np.zeros(t.shape, np.int16)
     # Vertical differences between rows i and i+1, then horizontal ones.
-    dv_s, dv_t = s[1:] - s[:-1], t[1:] - t[:-1]
-    grad[1:] += mix(dv_s, dv_t, gradient)          # centre minus up
-    grad[:-1] += mix(-dv_s, -dv_t, gradient)       # centre minus down
-    dh_s, dh_t = s[:, 1:] - s[:, :-1], t[:, 1:] - t[:, :-1]
-    grad[:, 1:] += mix(dh_s, dh_t, gradient)       # centre minus left
-    grad[:, :-1] += mix(-dh_s, -dh_t, gradient)    # centre minus right
-    grad[mc == 0] = 0
+    dv_s, dv_t = s[1:] - s[:-1], ti[1:] - ti[:-1]
+    acc[1:] += _mixed_int(dv_s, dv_t, gradient)          # centre minus up
+    acc[:-1] += _mixed_int(-dv_s, -dv_t, gradient)       # centre minus down
+    dh_s, dh_t = s[:, 1:] - s[:, :-1], ti[:, 1:] - ti[:, :-1]
+    acc[:, 1:] += _mixed_int(dh_s, dh_t, gradient)       # centre minus left
+    acc[:, :-1] += _mixed_int(-dh_s, -dh_t, gradient)    # centre minus right
+    acc[mc == 0] = 0
+    grad = acc.astype(np.float32)
+    if _scale(gradient) != 1:
+        grad *= np.float32(1.0 / _scale(gradient))
     on_tgt = Crop(mask_on_tgt[0] + cr.x0, mask_on_tgt[0] + cr.x1,
                   mask_on_tgt[1] + cr.y0, mask_on_tgt[1] + cr.y1)
     return mc, t, grad, on_tgt
@@ -147,29 +172,34 @@ def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) ->
     sr, sc_ = mask_on_src[0] + cr.x0, mask_on_src[1] + cr.y0
     tr, tc_ = mask_on_tgt[0] + cr.x0, mask_on_tgt[1] + cr.y0
     n, m = mc.shape
-    s = src[sr:sr + n, sc_:sc_ + m].astype(np.float32)
-    t = tgt[tr:tr + n, tc_:tc_ + m].astype(np.float32)
+    s = src[sr:sr + n, sc_:sc_ + m].astype(np.int16)
+    t = tgt[tr:tr + n, tc_:tc_ + m].astype(np.int16)
     # Interior [1:-1, 1:-1] of the crop and its four shifted neighbours.
     inner = (slice(1, n - 1), slice(1, m - 1))
     shifts = {"L": (slice(1, n - 1), slice(0, m - 2)), "R": (slice(1, n - 1), slice(2, m)),
               "U": (slice(0, n - 2), slice(1, m - 1)), "D": (slice(2, n), slice(1, m - 1))}
     s0, t0 = s[inner], t[inner]
-    grad = None
+    # Integer terms, times k (see _mixed_int): exact, so the sums equal the
+    # reference's float32 sums in its order (L, R, U, D, then the unmasked
+    # neighbours' target values U, L, R, D).
+    k = _scale(gradient)
+    acc = None
     for d in ("L", "R", "U", "D"):
-        term = mix(s0 - s[shifts[d]], t0 - t[shifts[d]], gradient)
-        grad = term if grad is None else grad + term
-    bsum = grad
+        term = _mixed_int(s0 - s[shifts[d]], t0 - t[shifts[d]], gradient)
+        acc = term if acc is None else acc + term
     for d in ("U", "L", "R", "D"):
-        outside = np.broadcast_to((mc[shifts[d]] == 0)[..., None], bsum.shape)
-        np.add(bsum, t[shifts[d]], out=bsum, where=outside)
+        outside = np.broadcast_to((mc[shifts[d]] == 0)[..., None], acc.shape)
+        np.add(acc, t[shifts[d]] * np.int16(k), out=acc, where=outside)
     q = (px - 1) * (m - 2) + (py - 1)  # unknowns as flat indices of the interior
     A = np.zeros((N, 4), np.int32)
     X = np.zeros((N, 3), np.float32)
     B = np.zeros((N, 3), np.float32)
     X[1:] = np.ascontiguousarray(t0).reshape(-1, 3)[q]
-    for k, d in enumerate(("U", "D", "L", "R")):
-        A[1:, k] = np.ascontiguousarray(ids[shifts[d]]).reshape(-1)[q]
-    B[1:] = bsum.reshape(-1, 3)[q]
+    for j, d in enumerate(("U", "D", "L", "R")):
+        A[1:, j] = np.ascontiguousarray(ids[shifts[d]]).reshape(-1)[q]
+    B[1:] = acc.reshape(-1, 3)[q]
+    if k != 1:
+        B[1:] *= np.float32(1.0 / k)
     crop = Crop(mask_on_tgt[0] + cr.x0, mask_on_tgt[0] + cr.x1, mask_on_tgt[1] + cr.y0,
                 mask_on_tgt[1] + cr.y1)
     return EquSystem(N, A, X, B, (px + tr, py + tc_), crop)
