@@ -87,6 +87,14 @@ def _scale(gradient: str) -> int:
     return 2 if gradient == "avg" else 1
 
 
+def _arithmetic(src, tgt, gradient):
+    """(working dtype, mixer, scale): exact int16 terms for uint8 images
+    (the reference's inputs), else the reference's float32 arithmetic."""
+    if src.dtype == np.uint8 and tgt.dtype == np.uint8:
+        return np.int16, _mixed_int, _scale(gradient)
+    return np.float32, mix, 1
+
+
 def _check_offsets(shape, img_shape, off, crop: Crop, name: str) -> None:
     if (off[0] + crop.x0 < 0 or off[1] + crop.y0 < 0
             or off[0] + crop.x1 > img_shape[0] or off[1] + crop.y1 > img_shape[1]):
@@ -102,25 +110,26 @@ def grid_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient):
     _check_offsets(mask.shape[:2], src.shape, mask_on_src, cr, "source")
     _check_offsets(mask.shape[:2], tgt.shape, mask_on_tgt, cr, "target")
     mc = m01[cr.x0:cr.x1, cr.y0:cr.y1]
+    # uint8 images: exact integer terms (see _mixed_int), the same values as
+    # the reference's float32 arithmetic; other dtypes: that arithmetic.
+    work, mixer, k = _arithmetic(src, tgt, gradient)
     s = src[mask_on_src[0] + cr.x0:mask_on_src[0] + cr.x1,
-            mask_on_src[1] + cr.y0:mask_on_src[1] + cr.y1].astype(np.int16)
+            mask_on_src[1] + cr.y0:mask_on_src[1] + cr.y1].astype(work)
     ti = tgt[mask_on_tgt[0] + cr.x0:mask_on_tgt[0] + cr.x1,
-             mask_on_tgt[1] + cr.y0:mask_on_tgt[1] + cr.y1].astype(np.int16)
+             mask_on_tgt[1] + cr.y0:mask_on_tgt[1] + cr.y1].astype(work)
     t = ti.astype(np.float32)
-    # Integer terms (see _mixed_int): the same values as the float32
-    # arithmetic of the reference, computed without rounding.
-    acc = np.zeros(t.shape, np.int16)
+    acc = np.zeros(t.shape, work)
     # Vertical differences between rows i and i+1, then horizontal ones.
     dv_s, dv_t = s[1:] - s[:-1], ti[1:] - ti[:-1]
-    acc[1:] += _mixed_int(dv_s, dv_t, gradient)          # centre minus up
-    acc[:-1] += _mixed_int(-dv_s, -dv_t, gradient)       # centre minus down
+    acc[1:] += mixer(dv_s, dv_t, gradient)          # centre minus up
+    acc[:-1] += mixer(-dv_s, -dv_t, gradient)       # centre minus down
     dh_s, dh_t = s[:, 1:] - s[:, :-1], ti[:, 1:] - ti[:, :-1]
-    acc[:, 1:] += _mixed_int(dh_s, dh_t, gradient)       # centre minus left
-    acc[:, :-1] += _mixed_int(-dh_s, -dh_t, gradient)    # centre minus right
+    acc[:, 1:] += mixer(dh_s, dh_t, gradient)       # centre minus left
+    acc[:, :-1] += mixer(-dh_s, -dh_t, gradient)    # centre minus right
     acc[mc == 0] = 0
     grad = acc.astype(np.float32)
-    if _scale(gradient) != 1:
-        grad *= np.float32(1.0 / _scale(gradient))
+    if k != 1:
+        grad *= np.float32(1.0 / k)
     on_tgt = Crop(mask_on_tgt[0] + cr.x0, mask_on_tgt[0] + cr.x1,
                   mask_on_tgt[1] + cr.y0, mask_on_tgt[1] + cr.y1)
     return mc, t, grad, on_tgt
@@ -172,24 +181,25 @@ def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) ->
     sr, sc_ = mask_on_src[0] + cr.x0, mask_on_src[1] + cr.y0
     tr, tc_ = mask_on_tgt[0] + cr.x0, mask_on_tgt[1] + cr.y0
     n, m = mc.shape
-    s = src[sr:sr + n, sc_:sc_ + m].astype(np.int16)
-    t = tgt[tr:tr + n, tc_:tc_ + m].astype(np.int16)
+    work, mixer, k = _arithmetic(src, tgt, gradient)
+    s = src[sr:sr + n, sc_:sc_ + m].astype(work)
+    t = tgt[tr:tr + n, tc_:tc_ + m].astype(work)
     # Interior [1:-1, 1:-1] of the crop and its four shifted neighbours.
     inner = (slice(1, n - 1), slice(1, m - 1))
     shifts = {"L": (slice(1, n - 1), slice(0, m - 2)), "R": (slice(1, n - 1), slice(2, m)),
               "U": (slice(0, n - 2), slice(1, m - 1)), "D": (slice(2, n), slice(1, m - 1))}
     s0, t0 = s[inner], t[inner]
-    # Integer terms, times k (see _mixed_int): exact, so the sums equal the
-    # reference's float32 sums in its order (L, R, U, D, then the unmasked
-    # neighbours' target values U, L, R, D).
-    k = _scale(gradient)
+    # uint8 images: integer terms, times k (see _mixed_int), exact, so the
+    # sums equal the reference's float32 sums in its order (L, R, U, D, then
+    # the unmasked neighbours' target values U, L, R, D); other dtypes: the
+    # reference's float32 arithmetic in that order.
     acc = None
     for d in ("L", "R", "U", "D"):
-        term = _mixed_int(s0 - s[shifts[d]], t0 - t[shifts[d]], gradient)
+        term = mixer(s0 - s[shifts[d]], t0 - t[shifts[d]], gradient)
         acc = term if acc is None else acc + term
     for d in ("U", "L", "R", "D"):
         outside = np.broadcast_to((mc[shifts[d]] == 0)[..., None], acc.shape)
-        np.add(acc, t[shifts[d]] * np.int16(k), out=acc, where=outside)
+        np.add(acc, t[shifts[d]] * work(k), out=acc, where=outside)
     q = (px - 1) * (m - 2) + (py - 1)  # unknowns as flat indices of the interior
     A = np.zeros((N, 4), np.int32)
     X = np.zeros((N, 3), np.float32)

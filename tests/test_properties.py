@@ -103,3 +103,23 @@ def test_equ_inputs_match_the_oracle(p, order):
     for k in ("A", "X", "B"):
         np.testing.assert_array_equal(e[k], getattr(s, k))
     np.testing.assert_array_equal(np.stack(e["tgt_index"]), np.stack(s.tgt_index))
+
+
+@settings(max_examples=25, deadline=None)
+@given(problems(), st.integers(0, 2**31 - 1))
+def test_float_images_take_the_float_arithmetic(p, seed):
+    """Images that are not uint8 (fractional values) go through the
+    reference's float32 arithmetic, not the exact-integer shortcut."""
+    src, mask, tgt, mode = p
+    rng = np.random.default_rng(seed)
+    fsrc = src.astype(np.float32) + rng.random(src.shape).astype(np.float32)
+    ftgt = tgt.astype(np.float32) * np.float32(0.77)
+    a = oprep.grid_inputs(fsrc, mask, ftgt, (0, 0), (0, 0), mode)
+    b = prep.grid_inputs(fsrc, mask, ftgt, (0, 0), (0, 0), mode)
+    for x, y in zip(a[:3], b[:3]):
+        np.testing.assert_array_equal(x, y)
+    e = oprep.equ_inputs(fsrc, mask, ftgt, (0, 0), (0, 0), mode)
+    s = prep.equ_inputs(fsrc, mask, ftgt, (0, 0), (0, 0), mode,
+                        lambda mc: np.cumsum((mc > 0).reshape(-1)).reshape(mc.shape))
+    for k in ("A", "X", "B"):
+        np.testing.assert_array_equal(e[k], getattr(s, k))
