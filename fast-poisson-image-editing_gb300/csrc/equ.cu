@@ -177,7 +177,7 @@ void grid_set_red_black(Solver* s, bool on);
 // is a 4-neighbour raster stencil, i.e. its unknowns can be placed on a grid
 // so that each one's grid neighbours are exactly its A entries (0 where the
 // grid pixel holds no unknown).  EquProcessor builds such systems from a
-// mask (fpie/process.py:253-265); then the equation sweep
+// mask (fpie/process.py:252-266); then the equation sweep
 // X' = ((((B + X[U]) + X[D]) + X[L]) + X[R]) / 4 is, operation for
 // operation, the grid sweep with grad = B and 0 at every pixel that is not
 // an unknown.  On success pos[i] (i >= 1) is unknown i's pixel, row-major in
@@ -719,7 +719,7 @@ struct EquSolverImpl : Solver {
   int* d_rows = nullptr;  // target coordinates of unknowns 1..N-1 (GPU reset)
   int* d_cols = nullptr;
 
-  // GPU-side counterpart of EquProcessor.reset (fpie/process.py:293-372):
+  // GPU-side counterpart of EquProcessor.reset (fpie/process.py:192-271):
   // ids, A, X, B and the unknowns' target coordinates from the uint8 images.
   // box_out: crop on the target (row0, row1, col0, col1); returns N.
   int reset_images(const uint8_t* src, int sh, int sw, const uint8_t* msk, int mh, int mw, int mch,

@@ -1,6 +1,6 @@
 // GPU-side construction of the grid solver's inputs from the three images.
 //
-// Same results as the host path (GridProcessor.reset, fpie/process.py:422-487),
+// Same results as the host path (GridProcessor.reset, fpie/process.py:321-386),
 // bit for bit:
 //   * mask: a 3-channel mask is "on" when its channel mean is >= 128, i.e.
 //     when the channel sum is >= 384 (exact for uint8); a 1-channel mask when
@@ -121,7 +121,7 @@ void launch_prep_grid(const PrepArgs& a, uint8_t* mask, float* xa, float* xb, fl
 
 // ---- equation form ---------------------------------------------------------------
 // ids: 1-based row-major ranks of the set pixels of the crop (the reference's
-// partition + ids[mask == 0] = 0, fpie/process.py:281-291), by a three-step
+// partition + ids[mask == 0] = 0, fpie/process.py:180-190), by a three-step
 // scan over blocks of kScanTile pixels.  Red-black numbering (the OpenMP
 // EquSolver's partition, fpie/core/openmp/equ.cc:22-56): the same scan over
 // the cells with odd row + col of the crop, then over the even ones, whose
@@ -239,7 +239,7 @@ __device__ __forceinline__ float mix_term2(float a, float b, int mode) {
 
 // Row id of every set pixel: A = ids of (up, down, left, right), X = target,
 // B = grad (L, R, U, D order) + target values of unset neighbours (U, L, R,
-// D order), and the pixel's target coordinates (fpie/process.py:328-370).
+// D order), and the pixel's target coordinates (fpie/process.py:227-269).
 __global__ void equ_build_kernel(EquPrepArgs P, int4* __restrict__ A, float* __restrict__ x0,
                                  float* __restrict__ x1, float* __restrict__ b,
                                  int* __restrict__ rows, int* __restrict__ cols) {

@@ -6,16 +6,16 @@ bit for bit:
 * mask: a 3-channel mask is averaged over channels and compared with 128
   (for integer masks this is ``channel sum >= 384``), the 1-pixel frame is
   cleared, and the problem is cropped to the set pixels' bounding box grown
-  by one pixel (fpie/process.py:310-325, :439-452);
+  by one pixel (fpie/process.py:209-224, :338-351);
 * gradient mixing 'src' / 'avg' / 'max' (BaseProcessor.mixgrad,
-  fpie/process.py:214-223), with ties in 'max' keeping the source term;
+  fpie/process.py:113-122), with ties in 'max' keeping the source term;
 * grid inputs: grad = mixed(C-U) + mixed(C-D) + mixed(C-L) + mixed(C-R)
-  summed in that order, zero outside the mask (fpie/process.py:455-479);
+  summed in that order, zero outside the mask (fpie/process.py:362-378);
 * equation inputs: ids from the solver's partition (row-major, or odd
   cells first in red-black order), A = ids of (up, down, left, right),
   grad summed (L, R, U, D), B = grad + target values of unmasked
   neighbours added (U, L, R, D), row 0 the constant 0 (fpie/process.py:
-  281-372).
+  180-190, 225-266).
 """
 
 from __future__ import annotations
@@ -159,7 +159,7 @@ def equ_inputs(src, mask, tgt, mask_on_src, mask_on_tgt, gradient, partition) ->
     """Build A/X/B; ``partition`` is the solver's id assignment (mask -> ids).
 
     The arithmetic is the reference's, per unknown and in its order
-    (fpie/process.py:321-372): the gradient sums the mixed L, R, U, D terms,
+    (fpie/process.py:225-266): the gradient sums the mixed L, R, U, D terms,
     B then adds the target value of each unmasked neighbour in U, L, R, D
     order.  It runs on whole slabs of the crop (every unknown lies inside
     the crop's 1-pixel frame) and gathers the unknowns' rows once, instead

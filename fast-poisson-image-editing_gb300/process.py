@@ -1,11 +1,11 @@
 """Processors and backend routing, mirroring ``fpie.process``.
 
 ``EquProcessor`` / ``GridProcessor`` take the same constructor arguments as
-the reference's (fpie/process.py:247-279, :384-420), build the solver inputs
+the reference's (fpie/process.py:149-178, :286-319), build the solver inputs
 on the host (``prep``), hand them to the backend solver through the plugin
 surface (``partition`` / ``reset`` / ``sync`` / ``step``) and merge the
-solver's uint8 result into a copy of the target (fpie/process.py:374-381,
-:489-496).
+solver's uint8 result into a copy of the target (fpie/process.py:273-280,
+:388-395).
 
 Backends (``ALL_BACKEND``, printed by ``--check-backend``):
 
@@ -18,7 +18,7 @@ Backends (``ALL_BACKEND``, printed by ``--check-backend``):
 * ``gb300-bf16`` -- iterative refinement, BF16 correction sweeps.
 
 An unknown or unavailable backend prints a hint and raises AssertionError,
-as the reference does (fpie/process.py:190-206).
+as the reference does (fpie/process.py:94-105).
 """
 
 from __future__ import annotations
@@ -113,7 +113,7 @@ class EquProcessor(BaseProcessor):
         self.device_prep = device_prep
 
     def mask2index(self, mask: np.ndarray):
-        """ids, N, and the unknowns' (row, col) in id order (fpie/process.py:281-291)."""
+        """ids, N, and the unknowns' (row, col) in id order (fpie/process.py:180-190)."""
         ids = np.asarray(self.core.partition(mask)).astype(np.int64)
         ids[mask == 0] = 0
         x, y = np.nonzero(mask)

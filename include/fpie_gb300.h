@@ -44,7 +44,7 @@ enum fpie_precision { FPIE_FP32 = 0, FPIE_MIXED_FP16 = 1, FPIE_MIXED_BF16 = 2 };
  * FPIE_ORDER_RED_BLACK: the reference's OpenMP EquSolver -- partition
  *   numbers the cells with odd row + col first, then the even ones
  *   (fpie/core/openmp/equ.cc:22-56); a sweep updates unknowns 1..n_mid-1 in
- *   place, then n_mid..N-1 reading the new values (equ.cc:107-118). */
+ *   place, then n_mid..N-1 reading the new values (openmp/equ.cc:107-118). */
 enum fpie_order { FPIE_ORDER_JACOBI = 0, FPIE_ORDER_RED_BLACK = 1 };
 
 /* Library version as 10000*major + 100*minor + patch. */
@@ -93,7 +93,7 @@ int fpie_equ_reset(fpie_solver* s, int N, const int32_t* A, const float* X,
 /* fpie_equ_reset with the caller's placement of the unknowns on a grid:
  * pos int32[N] (pos[0] ignored) = row * m + col of unknown i in an n x m
  * crop, every unknown off the crop's 1-pixel frame -- what EquProcessor
- * knows from its mask (fpie/process.py:321-372).  The placement is checked
+ * knows from its mask (fpie/process.py:180-190, 219-225).  The placement is checked
  * on the device (each unknown alone on its pixel, its four grid neighbours
  * exactly its A entries, row 0 the zero constant, in red-black order the
  * colour parity) instead of being searched for on the host; FPIE_ERR_ARG if
@@ -164,7 +164,7 @@ int fpie_equ_reset_device(fpie_solver* s, int N, const int32_t* A,
 int fpie_equ_step_device(fpie_solver* s, int iteration, uint8_t* x,
                          float* err);
 
-/* GPU-side counterpart of GridProcessor.reset (fpie/process.py:422-487):
+/* GPU-side counterpart of GridProcessor.reset (fpie/process.py:321-386):
  * builds the grid inputs from the uint8 images -- src [src_h][src_w][3],
  * mask [mask_h][mask_w][mask_channels] (1 or 3), tgt [tgt_h][tgt_w][3] --
  * the mask's placement (src_row, src_col) on the source and (tgt_row,
@@ -178,7 +178,7 @@ int fpie_grid_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int sr
                            const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
                            int tgt_row, int tgt_col, int gradient, int on_device, int* box);
 
-/* GPU-side counterpart of EquProcessor.reset (fpie/process.py:281-372):
+/* GPU-side counterpart of EquProcessor.reset (fpie/process.py:192-271):
  * partition (row-major ids of the set pixels, by a prefix scan), A, X, B,
  * with the same images, offsets and gradient codes as
  * fpie_grid_reset_images; bit-identical to the host construction.  N_out
@@ -190,7 +190,7 @@ int fpie_equ_reset_images(fpie_solver* s, const uint8_t* src, int src_h, int src
                           int* N_out);
 
 /* Target-image coordinates of unknowns 1..N-1 after fpie_equ_reset_images
- * (the processor's tgt_index, fpie/process.py:370): rows, cols int32[N-1]. */
+ * (the processor's tgt_index, fpie/process.py:269): rows, cols int32[N-1]. */
 int fpie_equ_get_index(fpie_solver* s, int32_t* rows, int32_t* cols);
 
 /* Copies the equation inputs the solver holds: A int32[N][4], B
@@ -200,7 +200,7 @@ int fpie_equ_get_inputs(fpie_solver* s, int32_t* A, float* B);
 /* How the EquSolver sweeps (reference: the equation sweep of
  * fpie/core/cuda/equ.cu:76-96 and fpie/np_solver.py:33-41).  "auto"
  * (default): a system that is a 4-neighbour raster stencil -- the ones
- * EquProcessor builds from a mask (fpie/process.py:253-265), row 0 constant
+ * EquProcessor builds from a mask (fpie/process.py:252-266), row 0 constant
  * and zero -- is placed on a grid and swept by the grid kernels (temporally
  * blocked, autotuned; same operations in the same order, so bit-identical
  * results), any other system by the gather kernel.  "gather": always the

@@ -1,8 +1,9 @@
 #!/usr/bin/env bash
 # Builds the reference fpie's own CPU solver modules (core_gcc, core_openmp)
 # and the device code of its CUDA solvers (cubins) from their sources under
-# /root/reference into oracle/_ref/, for use as a checker and comparison arm
-# only.  Needs pybind11 headers (pip package) and the reference tree;
+# the reference tree ($FPIE_REFERENCE; by default the read-only copy this
+# recipe was written against) into oracle/_ref/, for use as a checker and
+# comparison arm only.  Needs pybind11 headers (pip package) and the reference tree;
 # exits 0 without doing anything when either is missing (e.g. on a box that
 # only carries this repository).
 set -euo pipefail

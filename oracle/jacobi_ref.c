@@ -10,7 +10,7 @@
  *   equ sweep      fpie/np_solver.py:33-41   X' = (B + X[A0] + X[A1] + X[A2] + X[A3]) / 4
  *   equ residual   fpie/np_solver.py:42-50   r  = B + X[A0] + X[A1] + X[A2] + X[A3] - 4X
  *   clip           fpie/np_solver.py:51-54, 98-101 plus the uint8 store of
- *                  fpie/process.py:379, 494 (clamp to [0,255], truncate)
+ *                  fpie/process.py:278, 393 (clamp to [0,255], truncate)
  * Threading follows the reference OpenMP grid solver's static row split
  * (fpie/core/openmp/grid.cc:75-103), with rows as the unit of work.
  * Per-channel errors are accumulated in double.

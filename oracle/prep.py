@@ -5,12 +5,12 @@ This module restates, in plain numpy, how the reference processors turn
 check and the CPU-baseline leg of the benchmark may import it; the backend
 never calls it.
 
-* ``threshold_mask``      -- fpie/process.py:310-318 (also :439-447)
-* ``crop_box``            -- fpie/process.py:320-325 / :449-452
-* ``mix``                 -- BaseProcessor.mixgrad, fpie/process.py:214-223
-* ``grid_inputs``         -- GridProcessor.reset, fpie/process.py:422-487
+* ``threshold_mask``      -- fpie/process.py:209-217 (also :338-346)
+* ``crop_box``            -- fpie/process.py:219-224 / :348-351
+* ``mix``                 -- BaseProcessor.mixgrad, fpie/process.py:113-122
+* ``grid_inputs``         -- GridProcessor.reset, fpie/process.py:321-386
 * ``equ_inputs``          -- EquProcessor.mask2index + reset,
-                             fpie/process.py:281-372 with
+                             fpie/process.py:180-190, 192-271 with
                              np_solver.EquSolver.partition (np_solver.py:14-16)
 
 Pinned against vectors produced by the reference itself

@@ -6,7 +6,7 @@ its ``fpie/core/cuda/grid.cu`` and ``fpie/core/cuda/equ.cu`` (device code
 only, ``nvcc -cubin`` for sm_103a) into ``oracle/_ref/cuda/`` where the
 reference tree is present, and the cubins travel with the repository.  The
 host side is ``oracle/ref_cuda_host.c``, a restatement of the reference's
-``step`` loops (``fpie/core/cuda/grid.cu:133-153``, ``equ.cu:188-211``) over
+``step`` loops (``fpie/core/cuda/grid.cu:133-153``, ``fpie/core/cuda/equ.cu:189-211``) over
 the CUDA driver API, compiled here with gcc on first use.
 
 The reference's CUDA kernels update in place (each sweep reads neighbours
@@ -97,7 +97,7 @@ def _load() -> None:
 
 class RefCudaGrid:
     """The reference's CudaGridSolver (fpie/core/cuda/grid.cu) on the current
-    CUDA device: reset copies mask / tgt / grad in (post_reset, grid.cu:33-53),
+    CUDA device: reset copies mask / tgt / grad in (post_reset, fpie/core/cuda/grid.cu:33-52),
     step(n) is the reference's step."""
 
     def __init__(self, grid_x: int = 8, grid_y: int = 8):
@@ -152,7 +152,7 @@ class RefCudaGrid:
 
 class RefCudaEqu:
     """The reference's CudaEquSolver (fpie/core/cuda/equ.cu): reset copies
-    A / X / B in (post_reset, equ.cu:56-74), step(n) is the reference's step."""
+    A / X / B in (post_reset, fpie/core/cuda/equ.cu:56-74), step(n) is the reference's step."""
 
     def __init__(self, block_size: int = 1024):
         self.block_size = int(block_size)

@@ -11,11 +11,11 @@
  *     threads covering the N x M crop, device synchronize, then
  *     copy_img_grid_kernel and error_grid_kernel, synchronize, copy err and
  *     the image back;
- *   - CudaEquSolver::step (fpie/core/cuda/equ.cu:188-211): the same with
+ *   - CudaEquSolver::step (fpie/core/cuda/equ.cu:189-211): the same with
  *     iter_equ_kernel over unknowns 1..N-1 in 1-D blocks of block_size, then
  *     copy_X_equ_kernel, error_equ_kernel and error_sum_equ_kernel.
  * The device buffers (the reference's post_reset allocations,
- * grid.cu:33-53, equ.cu:56-74) are passed in by the caller.
+ * fpie/core/cuda/grid.cu:33-52, equ.cu:56-74) are passed in by the caller.
  * Every call returns a CUresult (0 = success).  Kernels run on `stream`. */
 #include <cuda.h>
 #include <stddef.h>

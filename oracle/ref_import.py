@@ -1,9 +1,10 @@
 """ORACLE (test infrastructure only): import the reference fpie for checking.
 
-Loads the reference's pure-Python package from its source tree (default
-/root/reference, or $FPIE_REFERENCE) as the module ``fpie``, with the compiled
-reference solver modules that oracle/build_ref.sh puts in oracle/_ref/fpie
-on its search path.  Returns None when the tree is absent, so callers skip.
+Loads the reference's pure-Python package from its source tree (the
+``root`` argument, else $FPIE_REFERENCE) as the module ``fpie``, with the
+compiled reference solver modules that oracle/build_ref.sh puts in
+oracle/_ref/fpie on its search path.  Returns None when no tree is given or
+it is absent, so callers skip.
 """
 
 from __future__ import annotations
@@ -16,10 +17,12 @@ import sys
 _HERE = pathlib.Path(__file__).resolve().parent
 
 
-def import_reference():
+def import_reference(root=None):
     """Return the reference ``fpie.process`` module, or None if unavailable."""
-    root = pathlib.Path(os.environ.get("FPIE_REFERENCE", "/root/reference"))
-    pkg = root / "fpie"
+    root = root or os.environ.get("FPIE_REFERENCE")
+    if not root:
+        return None
+    pkg = pathlib.Path(root) / "fpie"
     if not (pkg / "process.py").exists():
         return None
     if "fpie" not in sys.modules:

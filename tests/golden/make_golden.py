@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Generate golden vectors by running the reference fpie itself.
 
-Needs the reference source tree (default /root/reference, or
-$FPIE_REFERENCE) and, for the OpenMP vectors, its compiled modules from
+Needs the reference source tree ($FPIE_REFERENCE, by default the read-only
+copy this script was written against, /root/reference) and, for the OpenMP vectors, its compiled modules from
 oracle/build_ref.sh.  Writes tests/golden/*.npz; the tests only read those
 files, so they run where the reference is absent.
 
@@ -18,6 +18,7 @@ Usage: python tests/golden/make_golden.py
 
 from __future__ import annotations
 
+import os
 import pathlib
 import sys
 
@@ -94,7 +95,7 @@ def run_case(P, name, src, mask, tgt, mos, mot, gradient, checkpoints, omp=False
 
 
 def main() -> None:
-    P = import_reference()
+    P = import_reference(os.environ.get("FPIE_REFERENCE", "/root/reference"))
     if P is None:
         sys.exit("reference tree not found; set FPIE_REFERENCE")
     W = _workloads()

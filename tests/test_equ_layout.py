@@ -1,7 +1,7 @@
 """Placement of equation systems on a grid (host code, no GPU).
 
 An EquSolver system whose index table A is a 4-neighbour raster stencil --
-what EquProcessor builds from a mask (fpie/process.py:253-265) -- is swept
+what EquProcessor builds from a mask (fpie/process.py:252-266) -- is swept
 by the grid kernels; these tests pin the placement the library computes
 (fpie_equ_raster_layout) against the oracle's systems, and its refusals.
 """
