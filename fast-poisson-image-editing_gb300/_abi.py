@@ -92,7 +92,25 @@ _PROTOS: dict[str, tuple] = {
     "fpie_batch_kernel": ([_P, ctypes.c_char_p, _I], _I),
     "fpie_batch_set_spin_limit": ([_P, ctypes.c_longlong], _I),
     "fpie_batch_launch_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "fpie_batch_add_images": ([_P, _P, _I, _I, _P, _I, _I, _I, _P, _I, _I, _I, _I, _I, _I, _I,
+                               _I, ctypes.POINTER(_I), _P], _I),
+    "fpie_batch_run_async": ([_P, _I], _I),
+    "fpie_batch_wait": ([_P], _I),
+    "fpie_batch_norms_async": ([_P, _P, _I], _I),
+    "fpie_batch_norms_wait": ([_P, _P], _I),
+    "fpie_probe_fp32_rate": ([_P, _I, _I, ctypes.POINTER(ctypes.c_double)], _I),
 }
+
+
+PROBE_KINDS = {"fadd2": 0, "fmul2": 1, "ffma2": 2, "fadd": 3}
+
+
+def fp32_rate(kind: str = "fadd2", iters: int = 20000, stream: int = 0) -> float:
+    """FP32 operations per second of one kind of instruction on the current
+    device (one operation per value; see fpie_probe_fp32_rate)."""
+    out = ctypes.c_double(0)
+    call("fpie_probe_fp32_rate", _P(stream), PROBE_KINDS[kind], int(iters), ctypes.byref(out))
+    return out.value
 
 
 def library_path() -> pathlib.Path:

@@ -64,9 +64,47 @@ class BatchSolver:
         self._shape[jid.value] = (n_, m_)
         return jid.value
 
+    def add_images(self, src, mask, tgt, mask_on_src: tuple[int, int],
+                   mask_on_tgt: tuple[int, int], gradient: str, iterations: int):
+        """A job from uint8 images (host arrays), built as GridProcessor.reset
+        builds the grid inputs, on the GPU.  Returns (job id, crop box on the
+        target: row0, row1, col0, col1)."""
+        from .backend import _image_args
+
+        keep, args, mode, on_dev = _image_args(src, mask, tgt, gradient)
+        if on_dev:
+            raise _abi.FpieArgumentError("add_images takes host (numpy) images")
+        jid = ctypes.c_int(-1)
+        box = (ctypes.c_int * 4)()
+        _abi.call("fpie_batch_add_images", self._h, *args, int(mask_on_src[0]), int(mask_on_src[1]),
+                  int(mask_on_tgt[0]), int(mask_on_tgt[1]), mode, int(iterations), ctypes.byref(jid),
+                  box)
+        del keep
+        self._shape[jid.value] = (box[1] - box[0], box[3] - box[2])
+        return jid.value, tuple(box)
+
     def run(self, max_sweeps: int = -1) -> None:
         """Advance every job by min(max_sweeps, its remaining sweeps); -1 = to completion."""
         _abi.call("fpie_batch_run", self._h, int(max_sweeps))
+
+    def run_async(self, max_sweeps: int = -1) -> None:
+        """``run`` without waiting for the launch; ``wait`` joins it."""
+        _abi.call("fpie_batch_run_async", self._h, int(max_sweeps))
+
+    def wait(self) -> None:
+        _abi.call("fpie_batch_wait", self._h)
+
+    def norms_async(self, jobs: list[int]) -> None:
+        """Queue the norms of `jobs` (after the queued work); ``norms_wait`` returns them."""
+        self._norm_ids = np.ascontiguousarray(jobs, dtype=np.int32)
+        _abi.call("fpie_batch_norms_async", self._h,
+                  _ptr(self._norm_ids) if len(self._norm_ids) else None, len(self._norm_ids))
+
+    def norms_wait(self) -> np.ndarray:
+        """[count, 6] float64 of the last ``norms_async``, as ``norms``."""
+        out = np.empty((len(self._norm_ids), 6), np.float64)
+        _abi.call("fpie_batch_norms_wait", self._h, _ptr(out) if len(out) else None)
+        return out
 
     def progress(self, job: int) -> tuple[int, int]:
         d, t = ctypes.c_int(0), ctypes.c_int(0)

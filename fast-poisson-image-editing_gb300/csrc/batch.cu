@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "prep.cuh"
 #include "grid_kernels.cuh"
 #include "grid_mixed.cuh"
 #include "grid_tbp.cuh"
@@ -353,6 +354,18 @@ struct Batch {
   long long launches = 0;
   long long spin_limit = 1LL << 25;  // x ~128 ns sleeps: a few seconds at most
   int sms = 0;
+  // Images-in adds copy on a second stream (see add_images).
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t xfer_done = nullptr;
+  // Asynchronous runs: each launch's error flag lands in a pinned slot that
+  // wait() checks; kMaxPending launches may be in flight.
+  static constexpr int kMaxPending = 64;
+  int* h_errs = nullptr;
+  int n_pending = 0;
+  // Asynchronous norms: one pinned array, filled by one copy per call.
+  double* h_norms = nullptr;
+  int h_norms_cap = 0, norms_count = -1;
+  cudaEvent_t norms_done = nullptr;
 
   explicit Batch(size_t budget_bytes) : budget(budget_bytes) {
     FPIE_CUDA(cudaGetDevice(&device));
@@ -360,9 +373,31 @@ struct Batch {
     FPIE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   }
   ~Batch() {
-    cudaStreamSynchronize(stream);
     for (auto& j : jobs) free_job(j);
+    cudaStreamSynchronize(stream);
+    if (xfer) {
+      cudaStreamSynchronize(xfer);
+      cudaStreamDestroy(xfer);
+    }
+    if (xfer_done) cudaEventDestroy(xfer_done);
+    if (norms_done) cudaEventDestroy(norms_done);
+    cudaFreeHost(h_errs);
+    cudaFreeHost(h_norms);
     cudaStreamDestroy(stream);
+  }
+
+  // Job buffers come from the library's stream-ordered pool on the batch's
+  // stream, so that removing a job (cudaFreeAsync) never waits for the
+  // device: the memory returns to the pool once the work queued before the
+  // removal -- e.g. an epoch still running -- is done.
+  template <typename T>
+  void alloc(T** p, size_t bytes) {
+    void* q = nullptr;
+    FPIE_CUDA(cudaMallocFromPoolAsync(&q, bytes, scratch_pool(), stream));
+    *p = static_cast<T*>(q);
+  }
+  void release(void* p) {
+    if (p) cudaFreeAsync(p, stream);
   }
 
   int precision = FPIE_FP32;
@@ -377,17 +412,17 @@ struct Batch {
   }
 
   void free_job(BatchJob& j) {
-    cudaFree(j.x[0]);
-    cudaFree(j.x[1]);
-    cudaFree(j.g);
-    cudaFree(j.mask);
-    cudaFree(j.img);
-    cudaFree(j.parts);
-    cudaFree(j.err);
-    cudaFree(j.norm);
-    cudaFree(j.e[0]);
-    cudaFree(j.e[1]);
-    cudaFree(j.r);
+    release(j.x[0]);
+    release(j.x[1]);
+    release(j.g);
+    release(j.mask);
+    release(j.img);
+    release(j.parts);
+    release(j.err);
+    release(j.norm);
+    release(j.e[0]);
+    release(j.e[1]);
+    release(j.r);
     j.e[0] = j.e[1] = nullptr;
     j.r = nullptr;
     j.x[0] = j.x[1] = j.g = nullptr;
@@ -399,8 +434,10 @@ struct Batch {
     j.live = false;
   }
 
-  int add(int n, int m, const int32_t* hm, const float* ht, const float* hg, int iterations) {
-    FPIE_REQUIRE(n >= 1 && m >= 1 && hm && ht && hg, FPIE_ERR_ARG, "bad job arrays");
+  // A new job slot of an n x m grid with zeroed device buffers (stream-
+  // ordered on the batch's stream); the caller fills mask, x and grad.
+  int new_job(int n, int m, int iterations) {
+    FPIE_REQUIRE(n >= 1 && m >= 1, FPIE_ERR_ARG, "bad job size");
     FPIE_REQUIRE(iterations >= 0, FPIE_ERR_ARG, "negative sweep count");
     FPIE_REQUIRE((long long)n * m <= (1LL << 29), FPIE_ERR_ARG, "job too large");
     const size_t need = job_bytes(n, m, precision);
@@ -419,23 +456,21 @@ struct Batch {
     j.L = grid_launch(j.G);
     j.sweeps_total = iterations;
     j.sweeps_done = 0;
-    j.hmask.resize((size_t)n * m);
-    for (size_t k = 0; k < j.hmask.size(); ++k) j.hmask[k] = hm[k] != 0;
     const size_t pb = (size_t)j.G.plane * sizeof(float);
     try {
-      FPIE_CUDA(cudaMalloc(&j.x[0], 3 * pb));
-      FPIE_CUDA(cudaMalloc(&j.x[1], 3 * pb));
-      FPIE_CUDA(cudaMalloc(&j.g, 3 * pb));
-      FPIE_CUDA(cudaMalloc(&j.mask, (size_t)j.G.plane));
-      FPIE_CUDA(cudaMalloc(&j.img, (size_t)n * m * 3));
-      FPIE_CUDA(cudaMalloc(&j.parts, (size_t)j.L.nparts * 6 * sizeof(double)));
-      FPIE_CUDA(cudaMalloc(&j.err, 3 * sizeof(float)));
-      FPIE_CUDA(cudaMalloc(&j.norm, 6 * sizeof(double)));
+      alloc(&j.x[0], 3 * pb);
+      alloc(&j.x[1], 3 * pb);
+      alloc(&j.g, 3 * pb);
+      alloc(&j.mask, (size_t)j.G.plane);
+      alloc(&j.img, (size_t)n * m * 3);
+      alloc(&j.parts, (size_t)j.L.nparts * 6 * sizeof(double));
+      alloc(&j.err, 3 * sizeof(float));
+      alloc(&j.norm, 6 * sizeof(double));
       if (precision != FPIE_FP32) {
         const size_t eb = (size_t)j.G.plane * 3 * 2, rb = (size_t)j.G.plane * 3 * sizeof(float);
-        FPIE_CUDA(cudaMalloc(&j.e[0], eb));
-        FPIE_CUDA(cudaMalloc(&j.e[1], eb));
-        FPIE_CUDA(cudaMalloc(&j.r, rb));
+        alloc(&j.e[0], eb);
+        alloc(&j.e[1], eb);
+        alloc(&j.r, rb);
         FPIE_CUDA(cudaMemsetAsync(j.e[0], 0, eb, stream));
         FPIE_CUDA(cudaMemsetAsync(j.e[1], 0, eb, stream));
         FPIE_CUDA(cudaMemsetAsync(j.r, 0, rb, stream));
@@ -444,13 +479,30 @@ struct Batch {
       FPIE_CUDA(cudaMemsetAsync(j.x[1], 0, 3 * pb, stream));
       FPIE_CUDA(cudaMemsetAsync(j.g, 0, 3 * pb, stream));
       FPIE_CUDA(cudaMemsetAsync(j.mask, 0, (size_t)j.G.plane, stream));
+    } catch (...) {
+      free_job(j);
+      throw;
+    }
+    j.live = true;
+    j.bytes = need;
+    used += need;
+    return id;
+  }
+
+  int add(int n, int m, const int32_t* hm, const float* ht, const float* hg, int iterations) {
+    FPIE_REQUIRE(hm && ht && hg, FPIE_ERR_ARG, "bad job arrays");
+    const int id = new_job(n, m, iterations);
+    BatchJob& j = jobs[id];
+    j.hmask.resize((size_t)n * m);
+    for (size_t k = 0; k < j.hmask.size(); ++k) j.hmask[k] = hm[k] != 0;
+    try {
       const size_t px = (size_t)n * m;
       AsyncScratch scratch(px * 28, stream);
       char* stage = scratch.bytes();
       FPIE_CUDA(cudaMemcpyAsync(stage, hm, px * 4, cudaMemcpyHostToDevice, stream));
       FPIE_CUDA(cudaMemcpyAsync(stage + px * 4, ht, px * 12, cudaMemcpyHostToDevice, stream));
       FPIE_CUDA(cudaMemcpyAsync(stage + px * 16, hg, px * 12, cudaMemcpyHostToDevice, stream));
-      const int blocks = (int)std::min<long long>((px + 255) / 256, 152 * 16);
+      const int blocks = stride_blocks(px, 256, 16);
       batch_pack_kernel<<<blocks, 256, 0, stream>>>(
           j.G, reinterpret_cast<int32_t*>(stage), reinterpret_cast<float*>(stage + px * 4),
           reinterpret_cast<float*>(stage + px * 16), j.mask, j.x[0], j.x[1], j.g);
@@ -461,9 +513,93 @@ struct Batch {
       free_job(j);
       throw;
     }
-    j.live = true;
-    j.bytes = need;
-    used += need;
+    return id;
+  }
+
+  // A job from the three uint8 images, as GridProcessor.reset builds it
+  // (fpie/process.py:321-386): the mask is thresholded and its frame
+  // cleared on the host (a pass over mh x mw bytes that gives the crop, and
+  // the tile lists need the crop mask on the host anyway); the crop's
+  // gradient mixing and the planar layout are built on the device by the
+  // GPU-side reset's kernel (prep.cu).  The images are copied on a second
+  // stream, so the copies do not wait for an epoch running on the batch's
+  // stream; the build kernel is queued on the batch's stream after them.
+  // box = the crop on the target (row0, row1, col0, col1).
+  int add_images(const uint8_t* src, int sh, int sw, const uint8_t* msk, int mh, int mw,
+                 int mch, const uint8_t* tgt, int th, int tw, int s_row, int s_col, int t_row,
+                 int t_col, int mode, int iterations, int* box) {
+    FPIE_REQUIRE(src && msk && tgt, FPIE_ERR_ARG, "null input array");
+    FPIE_REQUIRE(sh > 0 && sw > 0 && mh > 0 && mw > 0 && th > 0 && tw > 0, FPIE_ERR_ARG,
+                 "empty image");
+    FPIE_REQUIRE(mch == 1 || mch == 3, FPIE_ERR_ARG, "mask must have 1 or 3 channels");
+    FPIE_REQUIRE(mode >= 0 && mode <= 2, FPIE_ERR_ARG,
+                 "gradient mode must be 0 (src), 1 (avg), 2 (max)");
+    std::vector<uint8_t> m01((size_t)mh * mw);
+    int b0 = INT32_MAX, b1 = -1, b2 = INT32_MAX, b3 = -1;
+    for (int i = 0; i < mh; ++i)
+      for (int k = 0; k < mw; ++k) {
+        const size_t p = (size_t)i * mw + k;
+        bool on = mch == 3 ? (int)msk[p * 3] + msk[p * 3 + 1] + msk[p * 3 + 2] >= 384
+                           : msk[p] >= 128;
+        on = on && i > 0 && i < mh - 1 && k > 0 && k < mw - 1;
+        m01[p] = on;
+        if (on) {
+          b0 = std::min(b0, i);
+          b1 = std::max(b1, i);
+          b2 = std::min(b2, k);
+          b3 = std::max(b3, k);
+        }
+      }
+    if (b1 < 0) throw Error{FPIE_ERR_ARG, "the mask selects no pixel (after clearing its 1-pixel frame)"};
+    const int x0 = b0 - 1, x1 = b1 + 2, y0 = b2 - 1, y1 = b3 + 2;
+    const bool fits = s_row + x0 >= 0 && s_col + y0 >= 0 && s_row + x1 <= sh && s_col + y1 <= sw &&
+                      t_row + x0 >= 0 && t_col + y0 >= 0 && t_row + x1 <= th && t_col + y1 <= tw;
+    if (!fits)
+      throw Error{FPIE_ERR_ARG,
+                  "the mask's crop at the given offsets leaves the source or target image"};
+    const int n = x1 - x0, m = y1 - y0;
+    const int id = new_job(n, m, iterations);
+    BatchJob& j = jobs[id];
+    j.hmask.resize((size_t)n * m);
+    for (int i = 0; i < n; ++i)
+      std::memcpy(&j.hmask[(size_t)i * m], &m01[(size_t)(x0 + i) * mw + y0], (size_t)m);
+    try {
+      if (!xfer) {
+        FPIE_CUDA(cudaStreamCreateWithFlags(&xfer, cudaStreamNonBlocking));
+        FPIE_CUDA(cudaEventCreateWithFlags(&xfer_done, cudaEventDisableTiming));
+      }
+      const size_t sb = (size_t)sh * sw * 3, tb = (size_t)th * tw * 3, mb = (size_t)mh * mw;
+      auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+      char* stage = nullptr;
+      FPIE_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&stage), al(sb) + al(tb) + al(mb),
+                                        scratch_pool(), xfer));
+      FPIE_CUDA(cudaMemcpyAsync(stage, src, sb, cudaMemcpyHostToDevice, xfer));
+      FPIE_CUDA(cudaMemcpyAsync(stage + al(sb), tgt, tb, cudaMemcpyHostToDevice, xfer));
+      FPIE_CUDA(cudaMemcpyAsync(stage + al(sb) + al(tb), m01.data(), mb, cudaMemcpyHostToDevice,
+                                xfer));
+      FPIE_CUDA(cudaEventRecord(xfer_done, xfer));
+      FPIE_CUDA(cudaStreamWaitEvent(stream, xfer_done, 0));
+      const uint8_t* dsrc = reinterpret_cast<uint8_t*>(stage);
+      const uint8_t* dtgt = reinterpret_cast<uint8_t*>(stage + al(sb));
+      const uint8_t* dm01 = reinterpret_cast<uint8_t*>(stage + al(sb) + al(tb));
+      PrepArgs a{j.G, dm01, mw, x0, y0, dsrc, sw, s_row + x0, s_col + y0, dtgt, tw, t_row + x0,
+                 t_col + y0, mode};
+      launch_prep_grid(a, j.mask, j.x[0], j.x[1], j.g, stream);
+      FPIE_CUDA(cudaGetLastError());
+      ++launches;
+      FPIE_CUDA(cudaFreeAsync(stage, stream));  // after the build kernel
+      // The host copies are staged before cudaMemcpyAsync returns (pageable
+      // memory), so the caller may reuse its arrays now.
+    } catch (...) {
+      free_job(j);
+      throw;
+    }
+    if (box) {
+      box[0] = t_row + x0;
+      box[1] = t_row + x1;
+      box[2] = t_col + y0;
+      box[3] = t_col + y1;
+    }
     return id;
   }
 
@@ -524,7 +660,8 @@ struct Batch {
 
   // Runs `sweeps[id]` more sweeps of the listed jobs in one persistent launch
   // of variant v; returns the device milliseconds (measured with events).
-  float launch(const std::vector<int>& ids, const std::vector<int>& sw, int vi, bool time_it) {
+  float launch(const std::vector<int>& ids, const std::vector<int>& sw, int vi, bool time_it,
+               bool async = false) {
     const BatchVariant& v = batch_variants()[vi];
     std::vector<BJobDev> dj;
     std::vector<int2> tiles;
@@ -627,16 +764,27 @@ struct Batch {
       FPIE_CUDA(cudaGetLastError());
       ++launches;
       if (time_it) FPIE_CUDA(cudaEventRecord(e1, stream));
-      int herr = 0;
-      FPIE_CUDA(cudaMemcpyAsync(&herr, q.error, sizeof(int), cudaMemcpyDeviceToHost, stream));
-      FPIE_CUDA(cudaStreamSynchronize(stream));
-      if (time_it) {
-        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+      if (async && !time_it) {
+        // The flag is read by wait(); the queue tables are freed after the
+        // copy in stream order.  The jobs' bookkeeping below still applies.
+        if (!h_errs) FPIE_CUDA(cudaMallocHost(&h_errs, kMaxPending * sizeof(int)));
+        if (n_pending == kMaxPending) wait();
+        h_errs[n_pending] = 0;
+        FPIE_CUDA(cudaMemcpyAsync(&h_errs[n_pending], q.error, sizeof(int),
+                                  cudaMemcpyDeviceToHost, stream));
+        ++n_pending;
+      } else {
+        int herr = 0;
+        FPIE_CUDA(cudaMemcpyAsync(&herr, q.error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        FPIE_CUDA(cudaStreamSynchronize(stream));
+        if (time_it) {
+          FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+        }
+        FPIE_REQUIRE(herr == 0, FPIE_ERR_TIMEOUT,
+                     "batch kernel: a dependency wait exceeded its spin limit");
       }
-      FPIE_REQUIRE(herr == 0, FPIE_ERR_TIMEOUT,
-                   "batch kernel: a dependency wait exceeded its spin limit");
     }
     for (size_t k = 0; k < ids.size(); ++k) {
       BatchJob& j = jobs[ids[k]];
@@ -660,7 +808,7 @@ struct Batch {
   // Advances every live job by min(limit, its remaining sweeps); limit < 0
   // means "to completion".  Tunes the kernel on the first call with enough
   // work (each candidate runs 64 real sweeps of every job).
-  void run(int limit) {
+  void run(int limit, bool async = false) {
     std::vector<int> ids = live_ids();
     auto remaining = [&](int id) {
       const int rem = jobs[id].sweeps_total - jobs[id].sweeps_done;
@@ -691,13 +839,66 @@ struct Batch {
       if (budget_sweeps >= 0) rem = std::min(rem, std::max(0, budget_sweeps));
       if (rem > 0) { run_ids.push_back(id); sw.push_back(rem); }
     }
-    if (!run_ids.empty()) launch(run_ids, sw, variant, false);
+    if (!run_ids.empty()) launch(run_ids, sw, variant, false, async);
+  }
+
+  // Waits for everything queued on the batch's stream and checks the error
+  // flags of the asynchronous runs.
+  void wait() {
+    FPIE_CUDA(cudaStreamSynchronize(stream));
+    bool timed_out = false;
+    for (int k = 0; k < n_pending; ++k) timed_out = timed_out || h_errs[k] != 0;
+    n_pending = 0;
+    FPIE_REQUIRE(!timed_out, FPIE_ERR_TIMEOUT,
+                 "batch kernel: a dependency wait exceeded its spin limit");
+  }
+
+  // Queues the FP64 residual norms of the listed jobs' current states (one
+  // refine launch + one reduction per job) and one copy of all of them into
+  // a pinned array; norms_wait() waits for that copy only.
+  void norms_async(const int* ids, int count) {
+    FPIE_REQUIRE((ids || count == 0) && count >= 0, FPIE_ERR_ARG, "bad arguments");
+    if (count > h_norms_cap) {
+      if (h_norms) {
+        if (norms_done) FPIE_CUDA(cudaEventSynchronize(norms_done));
+        cudaFreeHost(h_norms);
+        h_norms = nullptr;
+      }
+      FPIE_CUDA(cudaMallocHost(&h_norms, 6 * sizeof(double) * (size_t)count));
+      h_norms_cap = count;
+    }
+    if (!norms_done) FPIE_CUDA(cudaEventCreateWithFlags(&norms_done, cudaEventDisableTiming));
+    if (count > 0) {
+      AsyncScratch dn(6 * sizeof(double) * (size_t)count, stream);
+      double* d = reinterpret_cast<double*>(dn.bytes());
+      for (int k = 0; k < count; ++k) {
+        BatchJob& j = job(ids[k]);
+        launch_refine(FPIE_FP32, j.L.sweep_grid, j.L.sweep_block, j.G, j.mask, j.g, j.x[j.cur],
+                      nullptr, nullptr, nullptr, j.parts, stream);
+        launch_norms_finalize(j.parts, j.L.nparts, d + 6 * (size_t)k, stream);
+        FPIE_CUDA(cudaGetLastError());
+        launches += 2;
+      }
+      FPIE_CUDA(cudaMemcpyAsync(h_norms, d, 6 * sizeof(double) * (size_t)count,
+                                cudaMemcpyDeviceToHost, stream));
+    }
+    FPIE_CUDA(cudaEventRecord(norms_done, stream));
+    norms_count = count;
+  }
+
+  void norms_wait(double* out) {
+    FPIE_REQUIRE(norms_count >= 0, FPIE_ERR_STATE, "no norms queued");
+    FPIE_REQUIRE(out != nullptr || norms_count == 0, FPIE_ERR_ARG, "null output array");
+    FPIE_CUDA(cudaEventSynchronize(norms_done));
+    if (norms_count > 0) std::memcpy(out, h_norms, 6 * sizeof(double) * (size_t)norms_count);
+    norms_count = -1;
   }
 
   // FP64 residual norms of the listed jobs' current states (one refine
   // launch + one reduction per job), copied to out[6 * k ...].
   void norms(const int* ids, int count, double* out) {
     FPIE_REQUIRE(ids && out && count >= 0, FPIE_ERR_ARG, "bad arguments");
+    wait();
     std::vector<double> h(6 * (size_t)std::max(count, 1));
     for (int k = 0; k < count; ++k) {
       BatchJob& j = job(ids[k]);
@@ -723,6 +924,7 @@ struct Batch {
 
   void result(int id, uint8_t* img, float* err) {
     FPIE_REQUIRE(img && err, FPIE_ERR_ARG, "null output array");
+    if (n_pending) wait();
     BatchJob& j = job(id);
     finish(id);
     FPIE_CUDA(cudaMemcpyAsync(img, j.img, (size_t)j.n * j.m * 3, cudaMemcpyDeviceToHost, stream));
@@ -732,6 +934,7 @@ struct Batch {
 
   void state(int id, float* out) {
     FPIE_REQUIRE(out, FPIE_ERR_ARG, "null output array");
+    if (n_pending) wait();
     BatchJob& j = job(id);
     const size_t plane_bytes = (size_t)j.G.plane * sizeof(float);
     std::vector<float> h(3 * (size_t)j.G.plane);
@@ -810,6 +1013,35 @@ int fpie_batch_run(fpie_batch* b, int max_sweeps) {
   return guarded([&] { batch_of(b)->run(max_sweeps); });
 }
 
+int fpie_batch_run_async(fpie_batch* b, int max_sweeps) {
+  return guarded([&] { batch_of(b)->run(max_sweeps, true); });
+}
+
+int fpie_batch_wait(fpie_batch* b) {
+  return guarded([&] { batch_of(b)->wait(); });
+}
+
+int fpie_batch_norms_async(fpie_batch* b, const int* jobs, int count) {
+  return guarded([&] { batch_of(b)->norms_async(jobs, count); });
+}
+
+int fpie_batch_norms_wait(fpie_batch* b, double* out) {
+  return guarded([&] { batch_of(b)->norms_wait(out); });
+}
+
+int fpie_batch_add_images(fpie_batch* b, const uint8_t* src, int src_h, int src_w,
+                          const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
+                          const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
+                          int tgt_row, int tgt_col, int gradient, int iterations, int* job_id,
+                          int* box) {
+  return guarded([&] {
+    const int id = batch_of(b)->add_images(src, src_h, src_w, mask, mask_h, mask_w,
+                                           mask_channels, tgt, tgt_h, tgt_w, src_row, src_col,
+                                           tgt_row, tgt_col, gradient, iterations, box);
+    if (job_id) *job_id = id;
+  });
+}
+
 int fpie_batch_progress(fpie_batch* b, int job, int* done, int* total) {
   return guarded([&] {
     BatchJob& j = batch_of(b)->job(job);
@@ -834,8 +1066,7 @@ int fpie_batch_remove(fpie_batch* b, int job) {
   return guarded([&] {
     Batch* h = batch_of(b);
     BatchJob& j = h->job(job);
-    FPIE_CUDA(cudaStreamSynchronize(h->stream));
-    h->free_job(j);
+    h->free_job(j);  // stream-ordered: after any work queued for the job
   });
 }
 

@@ -51,6 +51,12 @@ int guarded(F&& body) {
   }
 }
 
+// Blocks for a grid-stride loop over `total` elements, `threads` per block:
+// one block per `threads` elements, at most `per_sm` blocks per SM of the
+// current device (its multiprocessor count is read once per device), at
+// least 1.
+int stride_blocks(long long total, int threads, int per_sm);
+
 // Stream-ordered device scratch that is released on every exit path,
 // exceptions included (cudaFreeAsync on the stream it was allocated on).
 // The library's stream-ordered scratch pool on the current device.  Unlike

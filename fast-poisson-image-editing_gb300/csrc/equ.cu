@@ -13,11 +13,10 @@
 #include <vector>
 
 #include "common.cuh"
+#include "prep.cuh"
 
 namespace fpie {
 
-void launch_prep_mask(const uint8_t* mask, int mh, int mw, int mch, uint8_t* m01, int* box,
-                      cudaStream_t st);
 int launch_equ_ids(const uint8_t* m01, int mw, int x0, int y0, int n, int m, int* counts,
                    int* ids, cudaStream_t st, bool red_black);
 void launch_equ_build(const uint8_t* m01, int mw, int x0, int y0, int n, int m, const int* ids,
@@ -158,10 +157,7 @@ equ_finish_kernel(EquGeom E, const int4* __restrict__ A,
   }
 }
 
-static int conv_blocks(long long total) {
-  long long b = (total + 255) / 256;
-  return (int)std::max<long long>(1, std::min<long long>(b, 152 * 32));
-}
+static int conv_blocks(long long total) { return stride_blocks(total, 256, 32); }
 
 Solver* new_grid_solver(int grid_x, int grid_y);
 void grid_reset_from_equ(Solver* s, cudaStream_t st, int n, int m, int N, const int* pos,

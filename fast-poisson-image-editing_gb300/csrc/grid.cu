@@ -23,23 +23,9 @@
 #include "grid_flow.cuh"
 #include "grid_tma.cuh"
 #include "grid_tb.cuh"
+#include "prep.cuh"
 
 namespace fpie {
-
-struct PrepArgs {
-  GridGeom G;
-  const uint8_t* m01;
-  int mw, x0, y0;
-  const uint8_t* src;
-  int sw, sx, sy;
-  const uint8_t* tgt;
-  int tw, tx, ty;
-  int mode;
-};
-void launch_prep_mask(const uint8_t* mask, int mh, int mw, int mch, uint8_t* m01, int* box,
-                      cudaStream_t st);
-void launch_prep_grid(const PrepArgs& a, uint8_t* mask, float* xa, float* xb, float* g,
-                      cudaStream_t st);
 
 __global__ void grid_inputs_unpack_kernel(GridGeom G, const uint8_t* __restrict__ mask,
                                           const float* __restrict__ g,
@@ -130,10 +116,7 @@ __global__ void grid_unpack_kernel(GridGeom G, const float* __restrict__ x,
   }
 }
 
-static int conv_blocks(long long total) {
-  long long b = (total + 255) / 256;
-  return (int)std::max<long long>(1, std::min<long long>(b, 152 * 32));
-}
+static int conv_blocks(long long total) { return stride_blocks(total, 256, 32); }
 
 // ---- the solver object ----------------------------------------------------------
 

@@ -1,10 +1,10 @@
 // Grid step that allocates nothing: fpie_grid_step_noalloc.
 //
 // For callers that cannot allocate device memory at the point where they
-// need a Poisson step: code that runs while a CUDA stream is being captured
-// into a graph, hosts whose device memory belongs to their own pool
-// allocator, and latency-critical loops where cudaMalloc/cudaFree (which may
-// synchronize the device) are not acceptable.  They pass every input and
+// need a Poisson step: hosts whose device memory belongs to their own pool
+// allocator (memory taken behind its back breaks its accounting), and
+// latency-critical loops where cudaMalloc/cudaFree (which may synchronize
+// the device) are not acceptable.  They pass every input and
 // output buffer; the one buffer the step needs beyond those -- the second
 // Jacobi state and the residual partials -- is a fixed array in the
 // library's device image, sized for grids of at most kNoAllocMaxPixels
@@ -14,7 +14,9 @@
 // Layout is the reference's own ([n][m][3] float32 state, [n][m] int32
 // mask), so a caller needs no conversion.  Arithmetic is the numpy
 // backend's order, exactly as in the solver objects' kernels, so the state
-// after k sweeps is bit-identical to GridSolver's.
+// and image after k sweeps are bit-identical to GridSolver's; err sums the
+// same per-pixel terms in double in another fixed order (256-pixel blocks),
+// so it agrees with GridSolver's to float rounding.
 //
 // The scratch array is shared by every call on a device and keeps the last
 // call's contents; everything a call reads from it is written by that call
@@ -102,8 +104,11 @@ NoAllocScratch g_noalloc_dev[kNoAllocMaxDevices];
 
 // Device addresses of the scratch arrays on the current device.  The first
 // call on a device resolves them (cudaGetSymbolAddress, which also loads the
-// library's module on that device) and loads the kernels, so later calls --
-// including ones made while a stream is being captured -- do no set-up.
+// library's module on that device) and loads the kernels, so later calls do
+// no set-up; that first call should come before any stream capture.  The
+// addresses are kept for the life of the process, so the entry point must
+// not be used across a cudaDeviceReset of the device (the module would be
+// loaded again at other addresses).
 NoAllocScratch noalloc_scratch() {
   int dev = 0;
   FPIE_CUDA(cudaGetDevice(&dev));

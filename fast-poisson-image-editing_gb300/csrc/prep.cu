@@ -15,6 +15,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "prep.cuh"
 
 namespace fpie {
 
@@ -60,17 +61,6 @@ __device__ __forceinline__ float mix_term(float a, float b, int mode) {
   return fabsf(a) < fabsf(b) ? b : a;                  // 'max'
 }
 
-struct PrepArgs {
-  GridGeom G;
-  const uint8_t* m01;
-  int mw, x0, y0;  // mask width, crop origin in mask coordinates
-  const uint8_t* src;
-  int sw, sx, sy;  // source width, crop origin in source coordinates
-  const uint8_t* tgt;
-  int tw, tx, ty;  // target width, crop origin in target coordinates
-  int mode;
-};
-
 __global__ void prep_grid_kernel(PrepArgs A, uint8_t* __restrict__ mask, float* __restrict__ xa,
                                  float* __restrict__ xb, float* __restrict__ g) {
   const GridGeom& G = A.G;
@@ -106,14 +96,14 @@ __global__ void prep_grid_kernel(PrepArgs A, uint8_t* __restrict__ mask, float* 
 void launch_prep_mask(const uint8_t* mask, int mh, int mw, int mch, uint8_t* m01, int* box,
                       cudaStream_t st) {
   const long long total = (long long)mh * mw;
-  const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 152 * 16));
+  const int blocks = stride_blocks(total, 256, 16);
   prep_mask_kernel<<<blocks, 256, 0, st>>>(mask, mh, mw, mch, m01, box);
 }
 
 void launch_prep_grid(const PrepArgs& a, uint8_t* mask, float* xa, float* xb, float* g,
                       cudaStream_t st) {
   const long long total = (long long)a.G.n * a.G.m;
-  const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 152 * 32));
+  const int blocks = stride_blocks(total, 256, 32);
   prep_grid_kernel<<<blocks, 256, 0, st>>>(a, mask, xa, xb, g);
 }
 
@@ -309,7 +299,7 @@ void launch_equ_build(const uint8_t* m01, int mw, int x0, int y0, int n, int m, 
                       float* b, int* rows, int* cols, cudaStream_t st) {
   EquPrepArgs P{{m01, mw, x0, y0, n, m}, ids, src, sw, sx, sy, tgt, tw, tx, ty, mode, np};
   const long long total = (long long)n * m;
-  const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 152 * 32));
+  const int blocks = stride_blocks(total, 256, 32);
   equ_build_kernel<<<blocks, 256, 0, st>>>(P, A, xa, xb, b, rows, cols);
 }
 

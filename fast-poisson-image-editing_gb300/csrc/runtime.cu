@@ -1,5 +1,6 @@
 // Library-wide pieces of the C ABI: version, last-error string, device count,
 // stream/precision setters, destroy, and the fixed-order residual finalizer.
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -35,6 +36,22 @@ finalize_kernel(const double* __restrict__ parts, int nparts,
 void launch_finalize(const double* parts, int nparts, float* err,
                      cudaStream_t st) {
   finalize_kernel<<<1, 256, 0, st>>>(parts, nparts, err);
+}
+
+int stride_blocks(long long total, int threads, int per_sm) {
+  static std::mutex mu;
+  static int sms[64] = {};
+  int dev = 0;
+  FPIE_CUDA(cudaGetDevice(&dev));
+  FPIE_REQUIRE(dev >= 0 && dev < 64, FPIE_ERR_STATE, "device ordinal out of range");
+  int n;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!sms[dev]) FPIE_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev));
+    n = sms[dev];
+  }
+  const long long want = (total + threads - 1) / threads;
+  return (int)std::max<long long>(1, std::min<long long>(want, (long long)n * per_sm));
 }
 
 cudaMemPool_t scratch_pool() {

@@ -16,6 +16,10 @@ scaled to the configurations this backend is measured on):
   5000 sweeps.
 * ``circle1800`` -- 4096x4096 source and target, 16x16 base field, circle of
   radius 1800 (about 10.2 M unknowns), 'max' gradient.
+* ``circle450``  -- the same construction at 1024x1024, radius 450 (636,121
+  unknowns, 903x903 crop): the smallest circle paste on which plain FP32
+  Jacobi stalls above 0.5 intensity units of the converged solution (at
+  0.566), so the precision comparison runs on it in seconds.
 * ``jobs``       -- a seeded mix of uneven paste jobs (circles, squares and
   Gaussian-smoothed noise blobs) for the batched and serving forms.
 """
@@ -91,6 +95,13 @@ def circle1800(iterations: int = 0) -> Problem:
     return Problem("circle1800", src, disk_mask(4096, 4096, 1800), tgt, (0, 0), (0, 0), "max", iterations)
 
 
+def circle450(iterations: int = 0) -> Problem:
+    """1024x1024 paste with a radius-450 circle (636,121 unknowns)."""
+    src = smooth_image(5, 1024, 1024, 16)
+    tgt = smooth_image(6, 1024, 1024, 16)
+    return Problem("circle450", src, disk_mask(1024, 1024, 450), tgt, (0, 0), (0, 0), "max", iterations)
+
+
 def blob_mask(rng: np.random.Generator, h: int, w: int, sigma: float = 6.0) -> np.ndarray:
     """Gaussian-smoothed uniform noise thresholded at 0.5, as a 0/255 mask.
 
@@ -145,4 +156,5 @@ def job_mix(n_jobs: int = 256, seed: int = 7, min_box: int = 32, max_box: int = 
     return jobs
 
 
-WORKLOADS = {"circle256": circle256, "square800": square800, "circle1800": circle1800}
+WORKLOADS = {"circle256": circle256, "square800": square800, "circle450": circle450,
+             "circle1800": circle1800}

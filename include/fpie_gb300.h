@@ -274,18 +274,20 @@ int fpie_grid_kernel(fpie_solver* s, char* buf, int len);
 
 /* ---- allocation-free grid step ---------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
- * allocate device memory where they need a step -- code running while a
- * stream is captured into a CUDA graph, hosts whose device memory is owned
- * by their own pool allocator, and loops where cudaMalloc/cudaFree's
- * possible device synchronization is not acceptable.
+ * allocate device memory where they need a step -- hosts whose device
+ * memory is owned by their own pool allocator (a cudaMalloc behind its back
+ * breaks its accounting), and loops where cudaMalloc/cudaFree's possible
+ * device synchronization is not acceptable.
  *
  * Runs `iteration` Jacobi sweeps of a grid given in the reference layout,
  * all pointers in device memory of the calling thread's current device:
  * mask int32[n][m]; x float32[n][m][3], the state, updated in place; grad
  * float32[n][m][3].  Then, if non-NULL, writes the clipped image
  * img uint8[n][m][3] and the per-channel sum of |residual| err float32[3].
- * Work is enqueued on `stream` (NULL = legacy default stream).  Results
- * are bit-identical to GridSolver's after the same sweeps.
+ * Work is enqueued on `stream` (NULL = legacy default stream).  The state
+ * and the image are bit-identical to GridSolver's after the same sweeps;
+ * err is the same per-pixel |residual| summed in double in another fixed
+ * order, so it agrees to float rounding (rtol 1e-5 in the tests).
  *
  * Limit: n*m <= 262,144 pixels (e.g. 512 x 512); larger grids are rejected
  * with FPIE_ERR_ARG.  The second state buffer and the residual partials
@@ -294,6 +296,8 @@ int fpie_grid_kernel(fpie_solver* s, char* buf, int len);
  * a device resolves that array's address and loads the kernels; make it
  * before any stream capture.  Calls share the array, so calls whose GPU work
  * may overlap (other streams or threads) must be serialized by the caller.
+ * The resolved address is kept per device for the life of the process: do
+ * not call this across a cudaDeviceReset of that device.
  * Nothing here calls cudaMalloc, cudaFree or an allocating library routine. */
 int fpie_grid_step_noalloc(int n, int m, const int32_t* mask, float* x,
                            const float* grad, int iteration, uint8_t* img,
@@ -329,7 +333,31 @@ int fpie_batch_set_precision(fpie_batch* b, int precision);
 int fpie_batch_add(fpie_batch* b, int n, int m, const int32_t* mask,
                    const float* tgt, const float* grad, int iterations,
                    int* job_id);
+/* A job from the three uint8 images and the offsets, as
+ * fpie_grid_reset_images builds a grid solver's inputs (GridProcessor.reset,
+ * fpie/process.py:321-386): the mask is thresholded and its frame cleared
+ * on the host, the crop's gradient mixing and layout are built on the
+ * device.  The copies run on a second stream, so adding a job does not wait
+ * for a run in flight; the job joins the next run.  box (may be NULL)
+ * receives the crop on the target: row0, row1, col0, col1. */
+int fpie_batch_add_images(fpie_batch* b, const uint8_t* src, int src_h, int src_w,
+                          const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
+                          const uint8_t* tgt, int tgt_h, int tgt_w, int src_row, int src_col,
+                          int tgt_row, int tgt_col, int gradient, int iterations, int* job_id,
+                          int* box);
 int fpie_batch_run(fpie_batch* b, int max_sweeps);
+/* fpie_batch_run without waiting for the launch (the first run with enough
+ * work still tunes synchronously); fpie_batch_wait waits for all queued work
+ * and reports a dependency wait that exceeded its limit (FPIE_ERR_TIMEOUT).
+ * Jobs added or removed meanwhile take effect in stream order. */
+int fpie_batch_run_async(fpie_batch* b, int max_sweeps);
+int fpie_batch_wait(fpie_batch* b);
+/* fpie_batch_norms split in two: queue the norms of `count` jobs (after the
+ * work already queued) and one copy of them to pinned host memory; then wait
+ * for that copy only and receive them (6 doubles per job, as
+ * fpie_batch_norms). */
+int fpie_batch_norms_async(fpie_batch* b, const int* jobs, int count);
+int fpie_batch_norms_wait(fpie_batch* b, double* out);
 int fpie_batch_progress(fpie_batch* b, int job, int* done, int* total);
 /* Clipped uint8 image [n][m][3] and per-channel sum |residual| of a job. */
 int fpie_batch_result(fpie_batch* b, int job, uint8_t* img, float* err);
@@ -349,6 +377,15 @@ int fpie_batch_launch_count(fpie_batch* b, long long* count);
 /* Kernel launches this solver has issued since creation (sweeps, residual,
  * image, conversions), counted on the host. */
 int fpie_launch_count(fpie_solver* s, long long* count);
+
+/* ---- measurement ------------------------------------------------------------
+ * No counterpart in the reference: the denominator of the sweep kernels'
+ * compute roofline.  Times one launch of `iters` rounds of independent
+ * packed FP32 chains on every SM of the current device (CUDA events on
+ * `stream`) and writes the rate in operations per second, one operation
+ * per value: kind 0 packed add (__fadd2_rn), 1 packed multiply, 2 packed
+ * fused multiply-add (one operation per value), 3 scalar add. */
+int fpie_probe_fp32_rate(void* stream, int kind, int iters, double* ops_per_s);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,8 @@ GOLDEN_CASES = ["smoke6", "rand24", "circle256", "avg_offsets", "blob_frame"]
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # Enforced by the pytest-timeout plugin where it is installed.
+    config.addinivalue_line("markers", "timeout(seconds): fail the test after this many seconds")
 
 
 def load_golden(name: str) -> dict:
