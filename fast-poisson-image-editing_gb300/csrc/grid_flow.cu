@@ -150,17 +150,14 @@ __device__ __noinline__ void flow_rb_item(const FlowArgs& A, int tile, int c, in
       G, A.mask, A.g + co, A.x[pin] + co, A.x[pin ^ 1] + co, base, ks, lane, w, edge);
 }
 
-// Thread 0 keeps the next item's record and counters, loaded right after
-// the current item's sweeps so that their latency overlaps the release
-// fence and barrier; the other threads get tile and flag through shared
-// memory.
-// One item of the mixed forms at level z: the batched kernel's level
-// schedule (mixed_level: fold + first inner sweeps, inner sweeps on the
-// correction, final fold), on one (tile, channel).  Out of line like
-// flow_item.
+// The mixed forms' items at level z (the batched kernel's level schedule,
+// mixed_level: fold + first inner sweeps, inner sweeps on the correction,
+// final fold), one out-of-line function per level type so that each gets
+// the register assignment of its own body (one function holding all three
+// needed 255 registers and spilled).
 template <bool FULL, typename TS>
-__device__ __noinline__ void flow_mixed_item(const FlowArgs& A, int tile, int c, int z,
-                                             float4 (&edge)[2][2][kW][32], int lane, int w) {
+__device__ __noinline__ void flow_fold_item(const FlowArgs& A, int tile, int c, int cycle, int k,
+                                            float4 (&edge)[2][2][kW][32], int lane, int w) {
   const GridGeom& G = A.G;
   const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
   const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
@@ -168,31 +165,51 @@ __device__ __noinline__ void flow_mixed_item(const FlowArgs& A, int tile, int c,
   const float* gc = A.g + co;
   TS* e0 = static_cast<TS*>(A.e[0]);
   TS* e1 = static_cast<TS*>(A.e[1]);
-  const MixedLevel L = mixed_level(z, A.sweeps, kK);
-  if (L.type == 0) {
-    // x parity before this cycle's fold: one flip per earlier fold.
-    const int xp = (A.parity + (L.cycle > 0 ? L.cycle - 1 : 0)) & 1;
-    if (L.cycle > 0)  // full previous cycles end in e[1]
-      tbp_fold_body<kR, kW, kK, FULL, TS, true, true>(G, A.mask, gc, A.x[xp] + co, e1 + co,
-                                                      A.x[xp ^ 1] + co, A.r + co, e0 + co, base,
-                                                      L.k, lane, w, edge);
-    else
-      tbp_fold_body<kR, kW, kK, FULL, TS, false, true>(G, A.mask, gc, A.x[xp] + co, nullptr,
-                                                       nullptr, A.r + co, e0 + co, base, L.k,
-                                                       lane, w, edge);
-  } else if (L.type == 1) {
-    const TS* ein = ((L.pos - 1) & 1) ? e1 : e0;
-    TS* eout = (L.pos & 1) ? e1 : e0;
-    tbp_body<kR, kW, kK, FULL, TS, false, true>(G, A.mask, A.r + co, ein + co, eout + co, base,
-                                                L.k, lane, w, edge);
-  } else {
-    const int xp = (A.parity + L.cycle - 1) & 1;
-    const TS* elast = (((L.nlast - 1) & 1) ? e1 : e0) + co;
-    refine_tile<TS>(G, A.mask, gc, A.x[xp] + co, elast, A.x[xp ^ 1] + co, nullptr, ty * kTH,
-                    tx * kTW, kTH, kTW);
-  }
+  // x parity before this cycle's fold: one flip per earlier fold.
+  const int xp = (A.parity + (cycle > 0 ? cycle - 1 : 0)) & 1;
+  if (cycle > 0)  // full previous cycles end in e[1]
+    tbp_fold_body<kR, kW, kK, FULL, TS, true, true>(G, A.mask, gc, A.x[xp] + co, e1 + co,
+                                                    A.x[xp ^ 1] + co, A.r + co, e0 + co, base, k,
+                                                    lane, w, edge);
+  else
+    tbp_fold_body<kR, kW, kK, FULL, TS, false, true>(G, A.mask, gc, A.x[xp] + co, nullptr,
+                                                     nullptr, A.r + co, e0 + co, base, k, lane,
+                                                     w, edge);
 }
 
+template <bool FULL, typename TS>
+__device__ __noinline__ void flow_inner_item(const FlowArgs& A, int tile, int c, int pos, int k,
+                                             float4 (&edge)[2][2][kW][32], int lane, int w) {
+  const GridGeom& G = A.G;
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long co = c * G.plane;
+  TS* e0 = static_cast<TS*>(A.e[0]);
+  TS* e1 = static_cast<TS*>(A.e[1]);
+  const TS* ein = ((pos - 1) & 1) ? e1 : e0;
+  TS* eout = (pos & 1) ? e1 : e0;
+  tbp_body<kR, kW, kK, FULL, TS, false, true>(G, A.mask, A.r + co, ein + co, eout + co, base, k,
+                                              lane, w, edge);
+}
+
+template <typename TS>
+__device__ __noinline__ void flow_flush_item(const FlowArgs& A, int tile, int c, int cycle,
+                                             int nlast) {
+  const GridGeom& G = A.G;
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const long long co = c * G.plane;
+  TS* e0 = static_cast<TS*>(A.e[0]);
+  TS* e1 = static_cast<TS*>(A.e[1]);
+  const int xp = (A.parity + cycle - 1) & 1;
+  const TS* elast = (((nlast - 1) & 1) ? e1 : e0) + co;
+  refine_tile<TS>(G, A.mask, A.g + co, A.x[xp] + co, elast, A.x[xp ^ 1] + co, nullptr, ty * kTH,
+                  tx * kTW, kTH, kTW);
+}
+
+// Thread 0 keeps the next item's record and counters, loaded right after
+// the current item's sweeps so that their latency overlaps the release
+// fence and barrier; the other threads get tile and flag through shared
+// memory.
 // TS = float: the FP32 sweeps; __half / __nv_bfloat16: the mixed forms.
 template <typename TS>
 __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
@@ -226,11 +243,21 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
     __syncthreads();
     if (s_stop) break;
     const int tile = s_tile;
-    if (MIXED) {
-      if (s_flag == 2)
-        flow_mixed_item<true, TS>(A, tile, c, z, edge, lane, w);
-      else
-        flow_mixed_item<false, TS>(A, tile, c, z, edge, lane, w);
+    if constexpr (MIXED) {
+      const MixedLevel L = mixed_level(z, A.sweeps, kK);
+      if (L.type == 0) {
+        if (s_flag == 2)
+          flow_fold_item<true, TS>(A, tile, c, L.cycle, L.k, edge, lane, w);
+        else
+          flow_fold_item<false, TS>(A, tile, c, L.cycle, L.k, edge, lane, w);
+      } else if (L.type == 1) {
+        if (s_flag == 2)
+          flow_inner_item<true, TS>(A, tile, c, L.pos, L.k, edge, lane, w);
+        else
+          flow_inner_item<false, TS>(A, tile, c, L.pos, L.k, edge, lane, w);
+      } else {
+        flow_flush_item<TS>(A, tile, c, L.cycle, L.nlast);
+      }
     } else if (A.red_black) {
       if (s_flag == 2)
         flow_rb_item<true>(A, tile, c, z, edge, lane, w);
