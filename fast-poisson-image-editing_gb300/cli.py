@@ -19,7 +19,7 @@ import sys
 import time
 
 from . import __version__
-from .process import ALL_BACKEND, CPU_COUNT, DEFAULT_BACKEND
+from .process import ALL_BACKEND, BACKEND_NOTES, CPU_COUNT, DEFAULT_BACKEND
 
 
 def get_args(argv=None) -> argparse.Namespace:
@@ -60,6 +60,8 @@ def get_args(argv=None) -> argparse.Namespace:
         sys.exit(0)
     if args.check_backend:
         print(ALL_BACKEND)
+        for name in ALL_BACKEND:
+            print(f"  {name}: {BACKEND_NOTES[name]}")
         sys.exit(0)
     for name, path in (("Source", args.source), ("Target", args.target)):
         if not path or not os.path.exists(path):

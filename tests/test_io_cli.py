@@ -81,6 +81,10 @@ def test_cli_check_backend():
     r = subprocess.run([sys.executable, "-m", "fpie_gb300.cli", "--check-backend"], cwd=ROOT,
                        check=True, capture_output=True, text=True)
     assert "gb300" in r.stdout
+    # the reference's list on the first line, then when to pick each backend
+    first, *notes = r.stdout.strip().splitlines()
+    assert first.startswith("[") and len(notes) == first.count(",") + 1
+    assert any(n.strip().startswith("gb300-rb:") for n in notes)
 
 
 def test_cli_missing_source_exits_1(tmp_path):
