@@ -67,6 +67,8 @@ struct Lanes4<__nv_bfloat16, CG> {
   }
 };
 
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
 __device__ __forceinline__ float2 pick2(uint32_t ma, uint32_t mb, uint32_t bit,
                                         float2 upd, float2 old) {
   return make_float2((ma & bit) ? upd.x : old.x, (mb & bit) ? upd.y : old.y);
@@ -440,15 +442,28 @@ __device__ __forceinline__ void tbp_fold_body(const GridGeom& G, const uint8_t* 
                                     __shfl_up_sync(0xffffffffu, cur[3].y, 1));
       const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
                                     __shfl_down_sync(0xffffffffu, cur[0].y, 1));
+      // grid_res in packed form, the same IEEE operations in the same order:
+      // 4x - g as one fused multiply-add (4x is exact, so the single rounding
+      // equals grid_res's rounding of the subtraction), then four additions
+      // of the negated neighbours (a - b is a + (-b)).
+      const float2 four = make_float2(4.0f, 4.0f);
+      float2 t[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) t[j] = __ffma2_rn(cur[j], four, neg2(Gp[i][j]));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], neg2(up[j]));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], neg2(dn[j]));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], neg2(j > 0 ? cur[j - 1] : lf));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], neg2(j < 3 ? cur[j + 1] : rt));
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const float2 l = j > 0 ? cur[j - 1] : lf;
-        const float2 r = j < 3 ? cur[j + 1] : rt;
         const uint32_t bit = 0xffu << (8 * j);
-        const float ra = (mk[i] & bit) ? -grid_res(cur[j].x, Gp[i][j].x, up[j].x, dn[j].x, l.x, r.x) : 0.0f;
-        const float rb = (mk[i + H] & bit) ? -grid_res(cur[j].y, Gp[i][j].y, up[j].y, dn[j].y, l.y, r.y) : 0.0f;
         up[j] = cur[j];
-        Gp[i][j] = make_float2(ra, rb);  // the residual becomes the sweeps' right-hand side
+        // the residual becomes the sweeps' right-hand side
+        Gp[i][j] = make_float2((mk[i] & bit) ? -t[j].x : 0.0f, (mk[i + H] & bit) ? -t[j].y : 0.0f);
       }
     }
   }
