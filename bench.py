@@ -137,17 +137,14 @@ def measured_peak():
 
 def kernel_shape(kernel: str, sweeps: int):
     """(sweeps per launch, launches per step, region passes per launch) of a
-    grid sweep kernel, from its name: "sweep1"; "r/p<R>w<W>k<K>[s|t]" (K
-    sweeps per launch); "p16w8k16d" (dependency flow: the whole step in one
-    launch, a pass per 16-sweep level); "res16w8k4" (resident: the whole step
-    in one launch, one region load)."""
+    grid sweep kernel, from its name: "sweep1"; "p<R>w<W>k<K>[t]" (K sweeps
+    per launch); "p16w8k16d" / "rb16w8k8d" (dependency flow: the whole step
+    in one launch, a pass per level)."""
     if kernel == "sweep1":
         return 1, sweeps, 1
     depth = int(re.search(r"k(\d+)", kernel).group(1))
     if kernel.endswith("d"):
         return sweeps, 1, -(-sweeps // depth)
-    if kernel.startswith("res"):
-        return sweeps, 1, 1
     return depth, -(-sweeps // depth), 1
 
 
@@ -158,8 +155,8 @@ def apron_factor(kernel: str) -> float:
     """Region pixels a temporally blocked kernel sweeps per tile pixel it
     writes: regions are W*R rows x 128 columns, tiles lose K pixels (2K for
     red-black levels) on every side; 1 for the one-sweep kernel."""
-    m = re.match(r"(rb|p|r|res)(\d+)w(\d+)k(\d+)", kernel)
-    if not m or m.group(1) == "res":
+    m = re.match(r"(rb|p)(\d+)w(\d+)k(\d+)", kernel)
+    if not m:
         return 1.0
     r, w, k = (int(v) for v in m.groups()[1:])
     k = 2 * k if m.group(1) == "rb" else k

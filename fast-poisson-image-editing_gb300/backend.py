@@ -293,11 +293,11 @@ class GridSolver(_Solver):
         return img, err
 
     def set_kernel(self, name: str) -> None:
-        """Pin the sweep kernel ("auto", "sweep1", or a variant like "r16w8k8")."""
+        """Pin the sweep kernel ("auto", "sweep1", or a variant like "p16w8k16")."""
         _abi.call("fpie_grid_set_kernel", self._h, name.encode())
 
     def set_spin_limit(self, spins: int) -> None:
-        """Polls a resident-kernel neighbour wait, or a TMA-kernel copy wait,
+        """Polls a flow-kernel neighbourhood wait, or a TMA-kernel copy wait,
         may take before the step fails with FpieTimeoutError."""
         _abi.call("fpie_grid_set_spin_limit", self._h, ctypes.c_longlong(int(spins)))
 

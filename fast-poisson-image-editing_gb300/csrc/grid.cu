@@ -19,7 +19,6 @@
 #include "common.cuh"
 #include "grid_kernels.cuh"
 #include "grid_mixed.cuh"
-#include "grid_resident.cuh"
 #include "grid_flow.cuh"
 #include "grid_tma.cuh"
 #include "grid_tb.cuh"
@@ -138,28 +137,20 @@ struct GridSolverImpl : Solver {
   static constexpr int kChunk = 64;  // sweeps per captured graph (even)
   cudaGraphExec_t chunk[2] = {nullptr, nullptr};
 
-  // ---- resident kernel state (variant index kResident) -----------------------
-  static constexpr int kResident = -2;
-  int2* r_ctas = nullptr;
-  int* r_nbrs = nullptr;
-  int* r_counters = nullptr;  // [nctas] periods + [1] error flag
-  int r_nctas = 0, r_tiles_x = 0;
-  bool r_ok = false;          // lists built for the current mask
-  bool r_fits = false;        // every active (tile, channel) can be co-resident
-  int* h_rerr = nullptr;
-  long long r_spin_limit = 1LL << 26;  // x ~64 ns sleeps: a few seconds at most
+  // Bounded device waits (the flow kernel's neighbourhood waits, the TMA
+  // kernel's copy waits) give up after spin_limit rounds and set d_wait_err.
+  long long spin_limit = 1LL << 26;  // x ~64 ns sleeps: a few seconds at most
+  int* d_wait_err = nullptr;
+  int* h_wait_err = nullptr;  // pinned
 
-  // ---- persistent TMA-prefetch kernel (variant index kTma) -------------------
+  // ---- persistent TMA-prefetch kernel (variant index kTma; by name only) -----
   static constexpr int kTma = -3;
-  int* d_tma_err = nullptr;  // set by a copy wait that timed out
-  int* h_tma_err = nullptr;  // pinned
   int* tma_list = nullptr;   // active-tile list (count + indices)
   int tma_list_cap = 0;
   int tma_grid = 0;          // persistent CTAs for the current tiling
 
   // ---- dependency-flow kernel (FP32: variant kFlow; mixed: mvariant kFlow) ---
-  // Its tables depend only on the geometry and the mask; it shares the
-  // wait-error flag with the TMA kernel.
+  // Its tables depend only on the geometry and the mask.
   static constexpr int kFlow = -4;
   uint8_t* ft_flags = nullptr;  // tile flags for the flow tiling
   int* ft_list = nullptr;       // active-tile list (count + indices)
@@ -171,93 +162,21 @@ struct GridSolverImpl : Solver {
   bool ft_ok = false;
   int flow_grid = 0;
 
-  // Reads and clears the TMA kernel's time-out flag; call after the stream
-  // has been synchronised.
-  void check_tma() {
-    if (!d_tma_err) return;
-    FPIE_CUDA(cudaMemcpyAsync(h_tma_err, d_tma_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  // Reads and clears the wait-error flag (a flow-kernel neighbourhood wait
+  // or a TMA copy wait that gave up); call after the stream has been
+  // synchronised.
+  void check_waits() {
+    if (!d_wait_err) return;
+    FPIE_CUDA(cudaMemcpyAsync(h_wait_err, d_wait_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
-    if (*h_tma_err) {
-      *h_tma_err = 0;
-      FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
+    if (*h_wait_err) {
+      *h_wait_err = 0;
+      FPIE_CUDA(cudaMemsetAsync(d_wait_err, 0, sizeof(int), stream));
       FPIE_CUDA(cudaStreamSynchronize(stream));
-      throw Error{FPIE_ERR_TIMEOUT, "TMA sweep kernel: a wait for a region copy timed out"};
+      throw Error{FPIE_ERR_TIMEOUT, "sweep kernel: a bounded device wait gave up"};
     }
   }
-  void check_async() override { check_tma(); }
-
-  void release_resident() {
-    r_fits = false;
-    cudaFree(r_ctas);
-    cudaFree(r_nbrs);
-    cudaFree(r_counters);
-    r_ctas = nullptr;
-    r_nbrs = nullptr;
-    r_counters = nullptr;
-    r_nctas = 0;
-    r_ok = false;
-  }
-
-  // Builds the CTA and neighbour lists from the mask (device -> host copy of
-  // the mask plane, once per reset).  Returns false if the problem has more
-  // active (tile, channel) pairs than can be co-resident.  With no active
-  // tile at all it returns true and r_nctas = 0 (sweeps change nothing).
-  bool build_resident() {
-    if (r_ok) return r_fits;
-    release_resident();
-    const int th = resident_tile_h(), tw = resident_tile_w(), k = resident_depth();
-    const int tx = (G.m + tw - 1) / tw, ty = (G.n + th - 1) / th;
-    std::vector<uint8_t> hm((size_t)G.plane);
-    FPIE_CUDA(cudaMemcpyAsync(hm.data(), mask, (size_t)G.plane, cudaMemcpyDeviceToHost, stream));
-    FPIE_CUDA(cudaStreamSynchronize(stream));
-    std::vector<int> flag(tx * ty, 0);
-    for (int a = 0; a < ty; ++a)
-      for (int b = 0; b < tx; ++b) {
-        bool any = false, all = true;
-        for (int i = a * th - k; i < (a + 1) * th + k; ++i)
-          for (int j = b * tw - k; j < (b + 1) * tw + k; ++j) {
-            const bool in = i >= 0 && i < G.n && j >= 0 && j < G.m;
-            const bool on = in && hm[G.at(i, j)];
-            all = all && on;
-            if (on && i >= a * th && i < (a + 1) * th && j >= b * tw && j < (b + 1) * tw) any = true;
-          }
-        flag[a * tx + b] = any ? (all ? 2 : 1) : 0;
-      }
-    std::vector<int> index(tx * ty * 3, -1);
-    std::vector<int2> ctas;
-    for (int t = 0; t < tx * ty; ++t)
-      if (flag[t])
-        for (int c = 0; c < 3; ++c) {
-          index[t * 3 + c] = (int)ctas.size();
-          ctas.push_back(make_int2(t * 3 + c, flag[t]));
-        }
-    r_ok = true;
-    r_tiles_x = tx;
-    r_nctas = 0;
-    r_fits = (int)ctas.size() <= resident_max_ctas();
-    if (ctas.empty() || !r_fits) return r_fits;
-    std::vector<int> nb(ctas.size() * 8, -1);
-    for (size_t q = 0; q < ctas.size(); ++q) {
-      const int t = ctas[q].x / 3, c = ctas[q].x % 3, a = t / tx, b = t % tx;
-      int n = 0;
-      for (int da = -1; da <= 1; ++da)
-        for (int db = -1; db <= 1; ++db) {
-          if (!da && !db) continue;
-          const int aa = a + da, bb = b + db;
-          if (aa < 0 || aa >= ty || bb < 0 || bb >= tx) continue;
-          const int other = index[(aa * tx + bb) * 3 + c];
-          if (other >= 0) nb[q * 8 + n++] = other;
-        }
-    }
-    r_nctas = (int)ctas.size();
-    FPIE_CUDA(cudaMalloc(&r_ctas, sizeof(int2) * ctas.size()));
-    FPIE_CUDA(cudaMalloc(&r_nbrs, sizeof(int) * nb.size()));
-    FPIE_CUDA(cudaMalloc(&r_counters, sizeof(int) * (ctas.size() + 1)));
-    FPIE_CUDA(cudaMemcpyAsync(r_ctas, ctas.data(), sizeof(int2) * ctas.size(), cudaMemcpyHostToDevice, stream));
-    FPIE_CUDA(cudaMemcpyAsync(r_nbrs, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice, stream));
-    FPIE_CUDA(cudaStreamSynchronize(stream));
-    return true;
-  }
+  void check_async() override { check_waits(); }
 
   // All `iters` sweeps in one launch of the dependency-flow kernel.  A wait
   // that timed out is reported at the next host synchronisation.
@@ -265,7 +184,7 @@ struct GridSolverImpl : Solver {
     ensure_flow_tables();
     FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
     launch_flow(G, mask, g, x[0], x[1], cur, ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles,
-                iters, d_tma_err, r_spin_limit, flow_grid, stream, red_black);
+                iters, d_wait_err, spin_limit, flow_grid, stream, red_black);
     post_launch(this);
     const int per_level = red_black ? flow_rb_depth() : flow_depth();
     const int levels = (iters + per_level - 1) / per_level;
@@ -279,30 +198,11 @@ struct GridSolverImpl : Solver {
     ensure_flow_tables();
     FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
     launch_flow_mixed(G, mask, g, x[0], x[1], cur, precision == FPIE_MIXED_BF16, e[0], e[1], r,
-                      ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles, iters, d_tma_err,
-                      r_spin_limit, flow_grid, stream);
+                      ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles, iters, d_wait_err,
+                      spin_limit, flow_grid, stream);
     post_launch(this);
     if (flow_mixed_flips(iters) & 1) cur ^= 1;
     e_pending = false;
-  }
-
-  // All `iters` sweeps in one cooperative launch.
-  void run_resident(int iters) {
-    FPIE_REQUIRE(build_resident(), FPIE_ERR_ARG,
-                 "the resident kernel needs every active tile of every channel co-resident; "
-                 "this grid has too many tiles for it");
-    if (r_nctas == 0) return;  // no masked pixel: sweeps leave the state as it is
-    if (!h_rerr) FPIE_CUDA(cudaMallocHost(&h_rerr, sizeof(int)));
-    FPIE_CUDA(cudaMemsetAsync(r_counters, 0, sizeof(int) * (r_nctas + 1), stream));
-    launch_resident(G, mask, g, x[cur], x[cur ^ 1], r_ctas, r_nbrs, r_nctas, r_tiles_x, iters,
-                    r_counters, r_counters + r_nctas, r_spin_limit, stream);
-    post_launch(this);
-    FPIE_CUDA(cudaMemcpyAsync(h_rerr, r_counters + r_nctas, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    FPIE_CUDA(cudaStreamSynchronize(stream));
-    FPIE_REQUIRE(*h_rerr == 0, FPIE_ERR_TIMEOUT,
-                 "resident kernel: a neighbour wait exceeded its spin limit");
-    const int periods = (iters + resident_depth() - 1) / resident_depth();
-    if (periods & 1) cur ^= 1;
   }
 
   // ---- mixed-precision refinement state (allocated on first use) -----------
@@ -333,7 +233,6 @@ struct GridSolverImpl : Solver {
     if (h_err) cudaFreeHost(h_err);
     if (h_norm) cudaFreeHost(h_norm);
     if (h_box) cudaFreeHost(h_box);
-    if (h_rerr) cudaFreeHost(h_rerr);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -379,8 +278,7 @@ struct GridSolverImpl : Solver {
     flags_cap = 0;
     flags_ok = false;
     release_mixed();
-    release_resident();
-    cudaFree(d_tma_err);
+    cudaFree(d_wait_err);
     cudaFree(tma_list);
     cudaFree(flow_inv);
     cudaFree(flow_done);
@@ -394,9 +292,9 @@ struct GridSolverImpl : Solver {
     ft_list = nullptr;
     flow_cap = 0;
     ft_ok = false;
-    if (h_tma_err) cudaFreeHost(h_tma_err);
-    d_tma_err = nullptr;
-    h_tma_err = nullptr;
+    if (h_wait_err) cudaFreeHost(h_wait_err);
+    d_wait_err = nullptr;
+    h_wait_err = nullptr;
     tma_list = nullptr;
     tma_list_cap = 0;
     x[0] = x[1] = g = nullptr;
@@ -420,7 +318,6 @@ struct GridSolverImpl : Solver {
       flags_ok = false;  // the new mask may activate other tiles
       mflags_ok = false;
       ft_ok = false;
-      r_ok = false;
       return;
     }
     release();
@@ -563,7 +460,6 @@ struct GridSolverImpl : Solver {
     flags_ok = false;
     mflags_ok = false;
     ft_ok = false;
-    r_ok = false;
     box_out[0] = t_row + x0;
     box_out[1] = t_row + x1;
     box_out[2] = t_col + y0;
@@ -614,7 +510,7 @@ struct GridSolverImpl : Solver {
       ensure_flow_tables();
       return;
     }
-    // sweep1 / resident: no flags
+    // sweep1: no flags
     if (flags_ok || (variant < 0 && variant != kTma)) return;
     const bool tma = variant == kTma;
     const bool listed = tma;  // kernels that take the active-tile list
@@ -652,11 +548,11 @@ struct GridSolverImpl : Solver {
   }
 
   void ensure_wait_flag() {
-    if (d_tma_err) return;
-    FPIE_CUDA(cudaMalloc(&d_tma_err, sizeof(int)));
-    FPIE_CUDA(cudaMallocHost(&h_tma_err, sizeof(int)));
-    *h_tma_err = 0;
-    FPIE_CUDA(cudaMemsetAsync(d_tma_err, 0, sizeof(int), stream));
+    if (d_wait_err) return;
+    FPIE_CUDA(cudaMalloc(&d_wait_err, sizeof(int)));
+    FPIE_CUDA(cudaMallocHost(&h_wait_err, sizeof(int)));
+    *h_wait_err = 0;
+    FPIE_CUDA(cudaMemsetAsync(d_wait_err, 0, sizeof(int), stream));
   }
 
   // Flags, active-tile list, records and counters of the flow tiling.
@@ -721,8 +617,8 @@ struct GridSolverImpl : Solver {
   // k sweeps (k <= depth()) from buffer `from`; flips nothing (caller does).
   void launch_block(cudaStream_t st, int from, int k) {
     if (variant == kTma) {
-      launch_tma(G, mask, g, x[from], x[from ^ 1], flags, tma_list, tiles_x, tiles, k, d_tma_err,
-                 r_spin_limit, tma_grid, st);
+      launch_tma(G, mask, g, x[from], x[from ^ 1], flags, tma_list, tiles_x, tiles, k, d_wait_err,
+                 spin_limit, tma_grid, st);
     } else if (variant < 0) {
       launch_grid_sweep(L, G, mask, g, x[from], x[from ^ 1], st);
     } else {
@@ -781,11 +677,9 @@ struct GridSolverImpl : Solver {
       }
     }
     // Candidates: three packed temporally blocked variants, then the flow
-    // kernel and (when it fits) the resident kernel below.  The other
-    // variants (sweep1, the scalar "r" ones, the shallower or shared-grad
-    // packed ones, the TMA kernel) stay available by name but were never the
-    // fastest on a measured shape; timing them would only lengthen the first
-    // step.
+    // kernel below.  sweep1 (one sweep per launch, the baseline) and the TMA
+    // kernel stay available by name but were never the fastest on a
+    // measured shape; timing them would only lengthen the first step.
     static const char* const kTuned[] = {"p16w8k16", "p8w16k16", "p16w8k8"};
     std::vector<int> cands;
     for (int v = 0; v < (int)tb_variants().size(); ++v) {
@@ -840,26 +734,7 @@ struct GridSolverImpl : Solver {
           best = kFlow;
         }
       }
-      check_tma();
-    }
-    // The resident kernel (Jacobi only), when every active tile fits co-resident.
-    if (!red_black && build_resident() && r_nctas > 0 && iters - used >= (kTuneReps + 1) * kChunk) {
-      select_variant(kResident);
-      run_resident(kChunk);
-      used += kChunk;
-      for (int r = 0; r < kTuneReps; ++r) {
-        FPIE_CUDA(cudaEventRecord(e0, stream));
-        run_resident(kChunk);
-        FPIE_CUDA(cudaEventRecord(e1, stream));
-        FPIE_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        FPIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        used += kChunk;
-        if (ms < best_ms) {
-          best_ms = ms;
-          best = kResident;
-        }
-      }
+      check_waits();
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -878,10 +753,6 @@ struct GridSolverImpl : Solver {
       return;
     }
     if (!tuned && !pinned) iters -= autotune(iters);
-    if (variant == kResident) {
-      if (iters > 0) run_resident(iters);
-      return;
-    }
     if (variant == kFlow) {
       if (iters > 0) run_flow(iters);
       return;
@@ -1079,7 +950,7 @@ struct GridSolverImpl : Solver {
           best = kFlow;
         }
       }
-      check_tma();
+      check_waits();
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1176,7 +1047,6 @@ struct GridSolverImpl : Solver {
     }
     int v = -100;  // unknown
     if (name == "sweep1") v = -1;
-    if (name == "res16w8k4") v = kResident;
     if (name == "p16w8k16t") v = kTma;
     if (name == "p16w8k16d") v = kFlow;
     for (size_t k = 0; k < tb_variants().size(); ++k)
@@ -1189,7 +1059,6 @@ struct GridSolverImpl : Solver {
   std::string kernel_name() const {
     if (precision != FPIE_FP32)
       return mvariant == kFlow ? std::string("p16w8k16d") : std::string(mixed_variants()[mvariant].name);
-    if (variant == kResident) return std::string("res16w8k4");
     if (variant == kTma) return std::string("p16w8k16t");
     if (variant == kFlow && red_black) return std::string(tb_variants()[red_black_variant()].name) + "d";
     if (variant == kFlow) return std::string("p16w8k16d");
@@ -1228,7 +1097,7 @@ struct GridSolverImpl : Solver {
     FPIE_CUDA(cudaMemcpyAsync(img_out, d_img, bytes, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaMemcpyAsync(h_err, d_err, 3 * sizeof(float), cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
-    check_tma();
+    check_waits();
     std::memcpy(err_out, h_err, 3 * sizeof(float));
   }
 
@@ -1242,7 +1111,7 @@ struct GridSolverImpl : Solver {
     post_launch(this);
     FPIE_CUDA(cudaMemcpyAsync(out, tmp, total * 12, cudaMemcpyDeviceToHost, stream));
     FPIE_CUDA(cudaStreamSynchronize(stream));
-    check_tma();
+    check_waits();
   }
 };
 
@@ -1313,8 +1182,8 @@ int fpie_grid_set_spin_limit(fpie_solver* s, long long spins) {
   return guarded([&] {
     FPIE_REQUIRE(spins >= 0, FPIE_ERR_ARG, "spin limit must be >= 0");
     GridSolverImpl* h = grid_of(s);
-    if (spins != h->r_spin_limit) h->drop_graphs();  // captured TMA launches hold the limit
-    h->r_spin_limit = spins;
+    if (spins != h->spin_limit) h->drop_graphs();  // captured TMA launches hold the limit
+    h->spin_limit = spins;
   });
 }
 
@@ -1365,7 +1234,7 @@ void grid_set_red_black(Solver* s, bool on) { static_cast<GridSolverImpl*>(s)->s
 std::string grid_kernel_of(Solver* s) { return static_cast<GridSolverImpl*>(s)->kernel_name(); }
 void grid_set_spin(Solver* s, long long spins) {
   GridSolverImpl* h = static_cast<GridSolverImpl*>(s);
-  if (spins != h->r_spin_limit) h->drop_graphs();
-  h->r_spin_limit = spins;
+  if (spins != h->spin_limit) h->drop_graphs();
+  h->spin_limit = spins;
 }
 }  // namespace fpie

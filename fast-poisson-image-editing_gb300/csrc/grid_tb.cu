@@ -1,124 +1,28 @@
-// Temporally blocked grid sweep: up to K Jacobi sweeps per launch.
+// Registry of the temporally blocked grid sweep variants and the tile-flag
+// kernel they share.
 //
-// A CTA handles one channel plane of one tile.  It loads a 128-column x
-// (W*R)-row region (the tile plus a K-pixel apron on every side) into
-// registers: lane l of warp w owns columns 4l..4l+3 and rows w*R..w*R+R-1 of
-// the region, with their grad values and mask bits.  Each sweep then needs
-//   * left/right neighbours: the group's inner pixels from its own registers,
-//     the group's edge pixels from the adjacent lanes (warp shuffles);
-//   * up/down neighbours: the strip's inner rows from its own registers, the
-//     strip's first/last row from the warps above/below (shared memory,
-//     double-buffered by sweep parity so one barrier per sweep suffices).
-// Values near the region border go stale sweep by sweep (their neighbours
-// outside the region are not updated), but after k <= K sweeps every pixel
-// at least K away from the border is exact, so the tile interior is written
-// back and the apron discarded.  Arithmetic per pixel is exactly the
-// one-sweep kernel's (numpy order), so results are bit-identical for any K.
+// A variant (grid_tbp.cu: packed FP32x2 row pairs) handles one channel plane
+// of one tile per CTA: it loads a 128-column x (W*R)-row region -- the tile
+// plus a K-pixel apron on every side -- into registers, sweeps it K times
+// (left/right neighbours from the adjacent lanes by warp shuffles, up/down
+// neighbours from the warps above/below through shared memory, one barrier
+// per sweep), and writes back the tile interior: after k <= K sweeps every
+// pixel at least K away from the region border is exact.  Arithmetic per
+// pixel is the one-sweep kernel's (numpy order), so results are
+// bit-identical for any K.  HBM traffic per launch: x, grad and mask of the
+// region once in, the tile's x once out.
 //
-// HBM traffic per launch: x, grad and mask of the region once in, the tile's
-// x once out -- about 37/k bytes per pixel-sweep instead of 37.
+// Variants measured and removed (slower on every measured shape, kept out of
+// the library): the scalar one-value-per-lane "r" family (best r16w8k16:
+// 1.49 us/sweep on square800 against 1.32 for the packed p16w8k16), the
+// shallower and shared-grad packed ones (p8w12k8, p16w8k4, p12w12k8s,
+// p8w16k8s), and a one-launch kernel with tiles resident in registers for
+// the whole step (1.76 us/sweep: its per-period neighbour waits cost more
+// than the reloads they saved).
 #include "common.cuh"
 #include "grid_tb.cuh"
 
 namespace fpie {
-
-// One sweep over the strip in registers.  FULL: the whole region is masked,
-// so the per-pixel mask select is skipped (same arithmetic for set pixels).
-template <int R, int W, bool FULL, bool GS>
-__device__ __forceinline__ void tb_sweep(float4 (&x)[R], const float4 (&gg)[R],
-                                         const uint32_t (&mk)[R],
-                                         const float4* __restrict__ sg,
-                                         float4 prev, float4 below, int lane) {
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const float4 cur = x[r];
-    const float4 dn = r < R - 1 ? x[r + 1] : below;
-    const float lf = __shfl_up_sync(0xffffffffu, cur.w, 1);
-    const float rt = __shfl_down_sync(0xffffffffu, cur.x, 1);
-    const float4 g = GS ? sg[r * 32 + lane] : gg[r];
-    float4 o;
-    o.x = jacobi5(g.x, prev.x, dn.x, lf, cur.y);
-    o.y = jacobi5(g.y, prev.y, dn.y, cur.x, cur.z);
-    o.z = jacobi5(g.z, prev.z, dn.z, cur.y, cur.w);
-    o.w = jacobi5(g.w, prev.w, dn.w, cur.z, rt);
-    if (!FULL) {
-      const uint32_t m = mk[r];
-      o.x = (m & 0x000000ffu) ? o.x : cur.x;
-      o.y = (m & 0x0000ff00u) ? o.y : cur.y;
-      o.z = (m & 0x00ff0000u) ? o.z : cur.z;
-      o.w = (m & 0xff000000u) ? o.w : cur.w;
-    }
-    prev = cur;
-    x[r] = o;
-  }
-}
-
-// GS: the grad values live in shared memory (dynamic, W*R*32 float4)
-// instead of registers, which frees 4R registers per thread for taller
-// regions at the same occupancy.
-template <int R, int W, int K, bool GS>
-__global__ void __launch_bounds__(W * 32)
-grid_tb_kernel(GridGeom G, const uint8_t* __restrict__ mask,
-               const float* __restrict__ g, const float* __restrict__ xin,
-               float* __restrict__ xout, const uint8_t* __restrict__ active,
-               int tiles_x, int ksweeps) {
-  constexpr int TH = W * R - 2 * K;
-  constexpr int TW = 128 - 2 * K;
-  static_assert(K % 4 == 0 && K > 0 && K <= kPad, "apron must be a multiple of 4, at most kPad");
-  static_assert(TH > 0, "tile must have rows");
-  __shared__ float4 edge[2][2][W][32];  // [parity][0 = first row, 1 = last row][warp][lane]
-  extern __shared__ float4 sgrad[];     // GS only: [W*R rows][32 lanes]
-
-  const int tile = blockIdx.x;
-  const uint8_t flag = active[tile];
-  if (!flag) return;
-  const int c = blockIdx.y;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
-  const int row0 = ty * TH - K + w * R;    // crop row of this strip's first row
-  const int col0 = tx * TW - K + 4 * lane;  // crop column of this lane's first column
-  const long long base = G.at(row0, col0);
-  const float* xc = xin + c * G.plane;
-  const float* gc = g + c * G.plane;
-  float4* sg = sgrad + w * R * 32;
-
-  float4 x[R], gg[R];
-  uint32_t mk[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const long long p = base + (long long)r * G.pitch;
-    x[r] = ld4(xc + p);
-    if (GS)
-      sg[r * 32 + lane] = ld4(gc + p);
-    else
-      gg[r] = ld4(gc + p);
-    mk[r] = __ldg(reinterpret_cast<const unsigned int*>(mask + p));
-  }
-
-  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int s = 0; s < ksweeps; ++s) {
-    const int par = s & 1;
-    edge[par][0][w][lane] = x[0];
-    edge[par][1][w][lane] = x[R - 1];
-    __syncthreads();  // also orders the grad stores before the first sweep
-    const float4 prev = w > 0 ? edge[par][1][w - 1][lane] : zero;
-    const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
-    if (flag == 2)
-      tb_sweep<R, W, true, GS>(x, gg, mk, sg, prev, below, lane);
-    else
-      tb_sweep<R, W, false, GS>(x, gg, mk, sg, prev, below, lane);
-  }
-
-  if (lane >= K / 4 && lane < 32 - K / 4) {
-    float* oc = xout + c * G.plane;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int rr = w * R + r;  // region row
-      if (rr >= K && rr < W * R - K)
-        *reinterpret_cast<float4*>(oc + base + (long long)r * G.pitch) = x[r];
-    }
-  }
-}
 
 // flags[t] = 0: tile t's interior (clipped to the crop) has no masked pixel;
 // 2: every pixel of its region (interior plus a k-pixel apron, padding
@@ -147,60 +51,11 @@ __global__ void grid_tile_flags_kernel(GridGeom G, const uint8_t* __restrict__ m
   if (threadIdx.x == 0) flags[t] = any ? (all ? 2 : 1) : 0;
 }
 
-namespace {
-
-template <int R, int W, int K, bool GS>
-constexpr size_t tb_dyn_smem() {
-  return GS ? (size_t)W * R * 32 * sizeof(float4) : 0;
-}
-
-template <int R, int W, int K, bool GS>
-void prepare_tb() {
-  if (tb_dyn_smem<R, W, K, GS>() > 48 * 1024)
-    FPIE_CUDA(cudaFuncSetAttribute(grid_tb_kernel<R, W, K, GS>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)tb_dyn_smem<R, W, K, GS>()));
-}
-
-template <int R, int W, int K, bool GS>
-void launch_tb(const GridGeom& G, const uint8_t* mask, const float* g,
-               const float* xin, float* xout, const uint8_t* active,
-               int tiles_x, int tiles, int ksweeps, cudaStream_t st) {
-  grid_tb_kernel<R, W, K, GS><<<dim3(tiles, 3), W * 32, tb_dyn_smem<R, W, K, GS>(), st>>>(
-      G, mask, g, xin, xout, active, tiles_x, ksweeps);
-}
-
-template <int R, int W, int K, bool GS>
-TbVariant make_variant(const char* name) {
-  TbVariant v;
-  v.name = name;
-  v.rows_per_thread = R;
-  v.warps = W;
-  v.depth = K;
-  v.apron = K;
-  v.tile_h = W * R - 2 * K;
-  v.tile_w = 128 - 2 * K;
-  v.launch = &launch_tb<R, W, K, GS>;
-  v.prepare = &prepare_tb<R, W, K, GS>;
-  return v;
-}
-
-}  // namespace
-
 void append_packed_variants(std::vector<TbVariant>& v);  // grid_tbp.cu
 
 const std::vector<TbVariant>& tb_variants() {
   static const std::vector<TbVariant> v = [] {
-    std::vector<TbVariant> t = {
-        make_variant<8, 8, 8, false>("r8w8k8"),
-        make_variant<16, 8, 8, false>("r16w8k8"),
-        make_variant<8, 16, 8, false>("r8w16k8"),
-        make_variant<16, 8, 16, false>("r16w8k16"),
-        make_variant<8, 16, 16, false>("r8w16k16"),
-        make_variant<16, 10, 8, true>("r16w10k8s"),
-        make_variant<16, 12, 8, true>("r16w12k8s"),
-        make_variant<12, 16, 16, true>("r12w16k16s"),
-    };
+    std::vector<TbVariant> t;
     append_packed_variants(t);
     return t;
   }();

@@ -195,10 +195,6 @@ void append_packed_variants(std::vector<TbVariant>& v) {
   v.push_back(make_packed<16, 8, 8>("p16w8k8"));
   v.push_back(make_packed<16, 8, 16>("p16w8k16"));
   v.push_back(make_packed<8, 16, 16>("p8w16k16"));
-  v.push_back(make_packed<8, 12, 8>("p8w12k8"));
-  v.push_back(make_packed<16, 8, 4>("p16w8k4"));
-  v.push_back(make_packed<12, 12, 8, true>("p12w12k8s"));
-  v.push_back(make_packed<8, 16, 8, true>("p8w16k8s"));
   v.push_back(make_packed_rb<16, 8, 8>("rb16w8k8"));
 }
 

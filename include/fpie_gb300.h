@@ -254,19 +254,19 @@ int fpie_grid_solve(fpie_solver* s, double tol, int max_sweeps, int check_every,
 
 /* Selects the grid sweep kernel by name: "auto" (default: the autotuner
  * times the candidates on the first long step and keeps the fastest for this
- * grid shape), "sweep1" (one sweep per launch), a temporally blocked
- * variant "r<R>w<W>k<K>" / packed "p<R>w<W>k<K>[s]" (R rows per thread, W
- * warps, K sweeps per launch, s = grad in shared memory), or "res16w8k4"
- * (the whole step in one cooperative launch, tiles resident in registers).
- * Every choice gives bit-identical results. */
+ * grid shape), "sweep1" (one sweep per launch), a packed temporally
+ * blocked variant "p16w8k16", "p8w16k16" or "p16w8k8" (R rows per thread, W
+ * warps, K sweeps per launch), "p16w8k16d" (the whole step in one
+ * cooperative launch, items started by neighbourhood dependencies) or
+ * "p16w8k16t" (persistent CTAs prefetching each region by TMA).  Every
+ * choice gives bit-identical results. */
 int fpie_grid_set_kernel(fpie_solver* s, const char* name);
 
-/* The resident kernel ("res16w8k4", grids whose active tiles all fit
- * co-resident) waits for neighbour tiles between its 4-sweep periods; each
- * wait gives up after `spins` polls (~64 ns apart).  The TMA kernel
- * ("p16w8k16t") waits for its region copies; each wait gives up after
- * `spins` polls.  Either way the step (or fpie_sync) returns
- * FPIE_ERR_TIMEOUT, leaving the state undefined.  Default 2^26. */
+/* The dependency-flow kernel ("p16w8k16d") waits for neighbour tiles to
+ * finish the previous level, the TMA kernel ("p16w8k16t") for its region
+ * copies; each wait gives up after `spins` polls (~64 ns apart), and the
+ * step (or fpie_sync) then returns FPIE_ERR_TIMEOUT, leaving the state
+ * undefined.  Default 2^26. */
 int fpie_grid_set_spin_limit(fpie_solver* s, long long spins);
 
 /* Writes the current grid sweep kernel's name (NUL-terminated) into buf. */
