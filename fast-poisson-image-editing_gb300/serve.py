@@ -60,6 +60,7 @@ class Request:
     max_residual: float | None = None
     job: int | None = None
     box: tuple | None = None
+    error: str | None = None  # why the request was rejected (then img is None)
 
     def size_bound(self) -> tuple[int, int]:
         """Rows and columns of a grid at least as large as the request's crop."""
@@ -86,28 +87,43 @@ class Server:
         self.queue: collections.deque[Request] = collections.deque()
         self.active: dict[int, Request] = {}
         self.finished: list[Request] = []
+        self.rejected: list[Request] = []  # refused at admission (req.error says why)
         self.epochs = 0
         self.peak_active = 0
 
     def submit(self, req: Request) -> None:
         self.queue.append(req)
 
+    def _reject(self, req: Request, now: float, why: str) -> None:
+        req.error = why
+        req.done = now
+        self.rejected.append(req)
+
     def _admit(self, now: float) -> None:
+        from ._abi import FpieArgumentError
+
         while self.queue:
             req = self.queue[0]
             need = self.job_bytes(*req.size_bound())
             used, budget = self.batch.memory()
+            if need > budget:  # can never fit: refuse it, serve the rest
+                self.queue.popleft()
+                self._reject(req, now, f"needs {need} B, more than the whole budget of {budget:.0f} B")
+                continue
             if used + need > budget:
-                if not self.active:
-                    raise RuntimeError(f"request {req.rid} needs {need} B, more than the whole budget")
-                return
+                return  # waits for running requests to free memory
             self.queue.popleft()
-            if req.problem is not None:
-                pb = req.problem
-                req.job, req.box = self.batch.add_images(pb.src, pb.mask, pb.tgt, pb.mask_on_src,
-                                                         pb.mask_on_tgt, pb.gradient, self.max_sweeps)
-            else:
-                req.job = self.batch.add(req.mask, req.tgt, req.grad, self.max_sweeps)
+            try:
+                if req.problem is not None:
+                    pb = req.problem
+                    req.job, req.box = self.batch.add_images(pb.src, pb.mask, pb.tgt, pb.mask_on_src,
+                                                             pb.mask_on_tgt, pb.gradient,
+                                                             self.max_sweeps)
+                else:
+                    req.job = self.batch.add(req.mask, req.tgt, req.grad, self.max_sweeps)
+            except FpieArgumentError as exc:  # e.g. an empty mask, a crop off the image
+                self._reject(req, now, str(exc))
+                continue
             req.admitted = now
             self.active[req.job] = req
         self.peak_active = max(self.peak_active, len(self.active))
@@ -190,11 +206,14 @@ def run_workload(requests: list[Request], rate: float, seed: int = 0, **server_k
     unknowns = sum(_unknowns(r) * r.sweeps for r in srv.finished)
 
     def pct(xs):
+        if not xs:
+            return {"p50": None, "p95": None, "p99": None, "max": None}
         return {"p50": 1e3 * percentile(xs, 50), "p95": 1e3 * percentile(xs, 95),
                 "p99": 1e3 * percentile(xs, 99), "max": 1e3 * max(xs)}
 
     return {
         "requests": len(srv.finished),
+        "rejected": len(srv.rejected),
         "rate_per_s": rate,
         "wall_s": wall,
         "throughput_req_per_s": len(srv.finished) / wall,

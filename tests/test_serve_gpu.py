@@ -89,3 +89,20 @@ def test_poisson_replay_reports_latency_percentiles():
     assert stats["requests"] == 6
     lat = stats["latency_ms"]
     assert 0 < lat["p50"] <= lat["p95"] <= lat["p99"] <= lat["max"]
+
+
+def test_unservable_request_is_rejected_and_the_rest_served():
+    """An image request whose mask selects nothing (after its frame is
+    cleared) is refused at admission with the engine's message; the other
+    requests are served as usual."""
+    from fpie_gb300.serve import Request
+
+    reqs = _requests()[:3]
+    bad = reqs[1].problem
+    bad = type(bad)(bad.name, bad.src, bad.mask * 0, bad.tgt, bad.mask_on_src, bad.mask_on_tgt,
+                    bad.gradient, bad.iterations)
+    reqs[1] = Request(reqs[1].rid, problem=bad)
+    res, srv = _serve(reqs, budget_bytes=4e9, epoch_sweeps=128, tol=1e-3, max_sweeps=3000)
+    assert [r.rid for r in srv.rejected] == [reqs[1].rid]
+    assert "no pixel" in srv.rejected[0].error
+    assert sorted(res) == sorted(r.rid for r in reqs if r.rid != reqs[1].rid)

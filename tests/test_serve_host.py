@@ -78,8 +78,33 @@ def test_sweep_cap_retires_unconverged_requests():
     assert r.sweeps == 600 and r.max_residual > 1e-30
 
 
-def test_request_larger_than_budget_is_an_error():
-    srv = Server(batch=FakeBatch(budget=10), job_bytes=lambda n, m: n * m)
-    srv.submit(_req(0, 5, r0=1.0))
-    with pytest.raises(RuntimeError):
-        srv.step(lambda: 0.0)
+def test_request_larger_than_budget_is_rejected_and_the_rest_served():
+    fb = FakeBatch(budget=30)
+    srv = Server(epoch_sweeps=100, tol=1e-3, max_sweeps=10000, batch=fb, job_bytes=lambda n, m: n * m)
+    srv.submit(_req(0, 6, r0=1.0))   # 36 "bytes": can never fit
+    srv.submit(_req(1, 5, r0=8.0))   # 25: fits
+    t = iter(range(10**6))
+    srv.drain(lambda: float(next(t)))
+    assert [r.rid for r in srv.rejected] == [0] and "budget" in srv.rejected[0].error
+    assert [r.rid for r in srv.finished] == [1] and srv.finished[0].error is None
+
+
+def test_request_the_engine_refuses_is_rejected():
+    from fpie_gb300._abi import FpieArgumentError
+
+    class Refusing(FakeBatch):
+        def add(self, mask, tgt, grad, iterations):
+            if not mask.any():
+                raise FpieArgumentError("the mask selects no pixel")
+            return super().add(mask, tgt, grad, iterations)
+
+    fb = Refusing(budget=1000)
+    srv = Server(epoch_sweeps=100, tol=1e-3, max_sweeps=10000, batch=fb, job_bytes=lambda n, m: n * m)
+    empty = _req(0, 5, r0=1.0)
+    empty.mask[:] = 0
+    srv.submit(empty)
+    srv.submit(_req(1, 5, r0=4.0))
+    t = iter(range(10**6))
+    srv.drain(lambda: float(next(t)))
+    assert [r.rid for r in srv.rejected] == [0] and "no pixel" in srv.rejected[0].error
+    assert [r.rid for r in srv.finished] == [1]
