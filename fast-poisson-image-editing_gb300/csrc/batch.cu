@@ -64,6 +64,12 @@ struct BQueue {
   long long spin_limit;
 };
 
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 template <typename T>
 __device__ __forceinline__ int upper_bound_idx(const T* a, int n, T v) {
   int lo = 0, hi = n;  // first index with a[i] > v
@@ -166,7 +172,10 @@ batch_persistent_kernel(BQueue Q) {
       const int need = J.ntiles * 3 * z;
       long long spins = 0;
       int stop = 0;
-      while (*(volatile int*)(Q.done + j) < need) {
+      // Acquire loads: the read that sees the count orders the producers'
+      // writes before everything this thread does next, and the CTA barrier
+      // below carries that order to the other threads -- no separate fence.
+      while (ld_acquire_gpu(Q.done + j) < need) {
         if (*(volatile int*)Q.error) { stop = 1; break; }
         if (++spins > Q.spin_limit) {
           atomicExch(Q.error, 1);
@@ -175,7 +184,6 @@ batch_persistent_kernel(BQueue Q) {
         }
         __nanosleep(128);
       }
-      __threadfence();
       s_stop = stop;
       // The next item is taken now, so that the atomic's round trip
       // overlaps this item's sweeps.  (A CTA then holds two items; the
