@@ -596,8 +596,10 @@ struct Batch {
       FPIE_CUDA(cudaGetLastError());
       ++launches;
       FPIE_CUDA(cudaFreeAsync(stage, stream));  // after the build kernel
-      // The host copies are staged before cudaMemcpyAsync returns (pageable
-      // memory), so the caller may reuse its arrays now.
+      // The copies read host memory (the caller's images and m01, which goes
+      // out of scope here): wait for them -- only for them, the second
+      // stream holds nothing else -- so every host buffer may be reused.
+      FPIE_CUDA(cudaStreamSynchronize(xfer));
     } catch (...) {
       free_job(j);
       throw;

@@ -338,7 +338,8 @@ int fpie_batch_add(fpie_batch* b, int n, int m, const int32_t* mask,
  * fpie/process.py:321-386): the mask is thresholded and its frame cleared
  * on the host, the crop's gradient mixing and layout are built on the
  * device.  The copies run on a second stream, so adding a job does not wait
- * for a run in flight; the job joins the next run.  box (may be NULL)
+ * for a run in flight (only for its own copies: the caller's arrays may be
+ * reused on return); the job joins the next run.  box (may be NULL)
  * receives the crop on the target: row0, row1, col0, col1. */
 int fpie_batch_add_images(fpie_batch* b, const uint8_t* src, int src_h, int src_w,
                           const uint8_t* mask, int mask_h, int mask_w, int mask_channels,
