@@ -153,3 +153,44 @@ def test_mixed_batch_needs_precision_before_jobs():
     b.add(mc, t, g, it)
     with pytest.raises(_abi.FpieError):
         _abi.call("fpie_batch_set_precision", b._h, 1)
+
+
+@pytest.mark.parametrize("gradient", ["src", "avg", "max"])
+def test_add_images_equals_host_built_inputs(gradient):
+    """A job added from uint8 images (3-channel mask, offsets on both images)
+    holds the inputs the host construction of GridProcessor.reset gives, and
+    its result equals a GridSolver reset from those inputs."""
+    from fpie_gb300 import prep, workloads
+    from fpie_gb300.batch import BatchSolver
+
+    rng = np.random.default_rng(3)
+    src = workloads.smooth_image(21, 140, 150, 12)
+    tgt = workloads.smooth_image(22, 160, 170, 12)
+    mask = np.zeros((90, 100, 3), np.uint8)
+    mask[10:80, 15:90] = rng.integers(100, 256, (70, 75, 3), dtype=np.uint8)
+    mos, mot = (20, 30), (40, 35)
+    mc, t, g, box = prep.grid_inputs(src, mask, tgt, mos, mot, gradient)
+    b = BatchSolver(4e9)
+    jid, jbox = b.add_images(src, mask, tgt, mos, mot, gradient, 333)
+    assert jbox == (box.x0, box.x1, box.y0, box.y1)
+    b.run()
+    state, img, err = _alone(mc, t, g, 333)
+    np.testing.assert_array_equal(b.state(jid), state)
+    bimg, berr = b.result(jid)
+    np.testing.assert_array_equal(bimg, img)
+    np.testing.assert_allclose(berr, err, rtol=1e-5)
+
+
+def test_add_images_rejects_bad_input():
+    from fpie_gb300 import _abi, workloads
+    from fpie_gb300.batch import BatchSolver
+
+    src = workloads.smooth_image(1, 64, 64, 8)
+    b = BatchSolver(4e9)
+    empty = np.zeros((32, 32), np.uint8)
+    with pytest.raises(_abi.FpieArgumentError, match="no pixel"):
+        b.add_images(src, empty, src, (0, 0), (0, 0), "max", 10)
+    full = np.full((32, 32), 255, np.uint8)
+    with pytest.raises(_abi.FpieArgumentError, match="leaves"):
+        b.add_images(src, full, src, (50, 0), (0, 0), "max", 10)
+    assert b.memory()[0] == 0

@@ -71,3 +71,16 @@ def test_equ_edge_cases(n_unknowns):
         np.testing.assert_array_equal(s.state(), o.X)
         np.testing.assert_array_equal(x, o.image())
         np.testing.assert_allclose(err, o.err64(), rtol=1e-5, atol=1e-4)
+
+
+def test_fp32_probe_rate_is_plausible():
+    """The roofline's denominator: the packed-add rate lies between 25% and
+    200% of SMs x 128 lanes x 2.5 GHz (one operation per value)."""
+    torch = pytest.importorskip("torch")
+    from fpie_gb300 import _abi
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    nominal = sms * 128 * 2.5e9
+    for kind in ("fadd2", "ffma2", "fadd"):
+        rate = _abi.fp32_rate(kind, iters=2000)
+        assert 0.25 * nominal < rate < 2.0 * nominal, (kind, rate, nominal)

@@ -117,3 +117,16 @@ def test_equ_placement_follows_the_target_index(golden):
         np.testing.assert_array_equal(r + sysm.crop.x0, sysm.tgt_index[0])
         np.testing.assert_array_equal(c + sysm.crop.y0, sysm.tgt_index[1])
         assert (d["grid_mask"][r, c] != 0).all()
+
+
+def test_fp32_probe_rejects_bad_arguments_without_a_gpu_call():
+    """Argument checks come before any CUDA call (kind and iteration count)."""
+    from fpie_gb300 import _abi
+
+    import ctypes
+
+    out = ctypes.c_double(0)
+    lib = _abi.lib()
+    assert lib.fpie_probe_fp32_rate(None, 7, 100, ctypes.byref(out)) == _abi.FPIE_ERR_ARG
+    assert lib.fpie_probe_fp32_rate(None, 0, 0, ctypes.byref(out)) == _abi.FPIE_ERR_ARG
+    assert lib.fpie_probe_fp32_rate(None, 0, 100, None) == _abi.FPIE_ERR_ARG
