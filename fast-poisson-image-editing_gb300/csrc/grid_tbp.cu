@@ -194,6 +194,9 @@ const std::vector<MixedVariant>& mixed_variants() {
 void append_packed_variants(std::vector<TbVariant>& v) {
   v.push_back(make_packed<16, 8, 8>("p16w8k8"));
   v.push_back(make_packed<16, 8, 16>("p16w8k16"));
+  // Short regions (64 rows) for small grids: twice the tiles of the 128-row
+  // variants, so a small paste keeps more SMs busy.
+  v.push_back(make_packed<8, 8, 8>("p8w8k8"));
   v.push_back(make_packed<8, 16, 16>("p8w16k16"));
   v.push_back(make_packed_rb<16, 8, 8>("rb16w8k8"));
 }

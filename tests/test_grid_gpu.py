@@ -125,7 +125,7 @@ def test_tensor_handoff(backend):
     assert s.launches >= 4  # pack, sweeps, residual/image, finalize
 
 
-KERNELS = ["sweep1", "p16w8k8", "p16w8k16", "p8w16k16", "p16w8k16t", "p16w8k16d"]
+KERNELS = ["sweep1", "p16w8k8", "p16w8k16", "p8w16k16", "p8w8k8", "p16w8k16t", "p16w8k16d"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
