@@ -89,6 +89,7 @@ def parse_args():
                    help="headline line only: skip the precision, batch, serving and large-grid legs")
     p.add_argument("--jobs", type=int, default=256, help="batch: jobs; serve: requests per rate")
     p.add_argument("--rates", default="50,500,2000")
+    p.add_argument("--epoch", type=int, default=256, help="serve: sweeps per epoch")
     p.add_argument("--precision", choices=["fp32", "fp16", "bf16"], default="fp32",
                    help="batch/serve workloads: FP32 or a mixed form")
     return p.parse_args()
@@ -778,12 +779,12 @@ def extra_legs(line: dict, args, pb, stream, sysm) -> None:
 
 
 def serve_study(mix, n_requests: int = 1000, rates=(50.0, 500.0, 2000.0),
-                forms=("fp32", "fp16")) -> dict:
+                forms=("fp32", "fp16"), epoch: int = 256) -> dict:
     """Poisson arrivals of paste requests drawn (seeded, with replacement)
     from the 256-job mix, images in: each request's inputs are built on the
     GPU at admission, inside its latency.  Each request stops at a max
     residual of 1e-3 per channel or 10000 sweeps; 40 GB HBM budget;
-    256-sweep epochs."""
+    `epoch`-sweep epochs (the stop rule is checked after each)."""
     from fpie_gb300.serve import Request, run_workload
 
     rng = np.random.default_rng(11)
@@ -791,12 +792,12 @@ def serve_study(mix, n_requests: int = 1000, rates=(50.0, 500.0, 2000.0),
     out = {"workload": f"{n_requests} requests per rate drawn from the 256-job mix (boxes "
                        "log-uniform 32..1024, circles/squares/blobs, src|max gradient), images "
                        "in; stop at max|r| <= 1e-3 per channel or 10000 sweeps; 40 GB budget; "
-                       "256-sweep epochs; Poisson arrivals",
+                       f"{epoch}-sweep epochs; Poisson arrivals",
            "latency": "arrival to result on the host, input construction included"}
     for form in forms:
         for rate in rates:
             reqs = [Request(k, problem=mix[int(d)]) for k, d in enumerate(draws)]
-            r = run_workload(reqs, rate, seed=int(rate), budget_bytes=40e9, epoch_sweeps=256,
+            r = run_workload(reqs, rate, seed=int(rate), budget_bytes=40e9, epoch_sweeps=epoch,
                              tol=1e-3, max_sweeps=10000, precision=form)
             out[f"{form}@{int(rate)}"] = r
     return out
@@ -1225,7 +1226,8 @@ def run_serve(args):
     torch.cuda.set_device(0)
     mix = workloads.job_mix(n_jobs=256, seed=7)
     rates = tuple(float(r) for r in args.rates.split(","))
-    res = serve_study(mix, n_requests=args.jobs, rates=rates, forms=(args.precision,))
+    res = serve_study(mix, n_requests=args.jobs, rates=rates, forms=(args.precision,),
+                      epoch=args.epoch)
     best = max((v for k, v in res.items() if isinstance(v, dict)),
                key=lambda r: r["throughput_req_per_s"])
     line = {"metric": "p99 latency ms (and throughput)", "value": best["latency_ms"]["p99"],
