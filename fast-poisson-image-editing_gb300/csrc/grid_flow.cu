@@ -274,10 +274,12 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
       R = load_rec(A.rec + rn / 3);
       load_counters(A, R, rn % 3, v);
     }
-    // Release: the CTA barrier orders every thread's writes before thread
-    // 0's release reduction, which makes them visible before the count.
+    // Release: the CTA barrier orders every thread's writes before the
+    // release reduction, which makes them visible before the count.  Thread
+    // 32 issues it, not thread 0: thread 0's acquire fence at the next item
+    // would otherwise wait for this reduction to be performed at L2.
     __syncthreads();
-    if (threadIdx.x == 0) release_add(A.done + 3 * a + c);
+    if (threadIdx.x == 32) release_add(A.done + 3 * a + c);
   }
 }
 
