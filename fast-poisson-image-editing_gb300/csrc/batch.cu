@@ -245,13 +245,13 @@ batch_persistent_kernel(BQueue Q) {
                         ty * TH, tx * TW, TH, TW);
       }
     }
-    // Release: the CTA barrier orders every thread's writes before thread
-    // 0's release reduction, which makes them visible before the count.
+    // Release: the CTA barrier orders every thread's writes before the
+    // release reduction, which makes them visible before the count.  Thread
+    // 32 issues it, so that thread 0's next acquire does not queue behind it.
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 32)
       asm volatile("red.release.gpu.global.add.s32 [%0], 1;" : : "l"(Q.done + j) : "memory");
-      s_idx = (long long)nxt;
-    }
+    if (threadIdx.x == 0) s_idx = (long long)nxt;
     __syncthreads();
   }
 }
