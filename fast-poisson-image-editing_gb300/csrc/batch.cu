@@ -245,14 +245,17 @@ batch_persistent_kernel(BQueue Q) {
                         ty * TH, tx * TW, TH, TW);
       }
     }
+    // The next index is published before the barrier below, which then
+    // serves both purposes: every thread reads it at the top of the next
+    // iteration (all reads of the current one happened before this item's
+    // first barrier), and every thread's writes precede the release.
+    if (threadIdx.x == 0) s_idx = (long long)nxt;
     // Release: the CTA barrier orders every thread's writes before the
     // release reduction, which makes them visible before the count.  Thread
     // 32 issues it, so that thread 0's next acquire does not queue behind it.
     __syncthreads();
     if (threadIdx.x == 32)
       asm volatile("red.release.gpu.global.add.s32 [%0], 1;" : : "l"(Q.done + j) : "memory");
-    if (threadIdx.x == 0) s_idx = (long long)nxt;
-    __syncthreads();
   }
 }
 
