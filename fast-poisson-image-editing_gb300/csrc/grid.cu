@@ -149,16 +149,23 @@ struct GridSolverImpl : Solver {
   int tma_list_cap = 0;
   int tma_grid = 0;          // persistent CTAs for the current tiling
 
-  // ---- dependency-flow kernel (FP32: variant kFlow; mixed: mvariant kFlow) ---
-  // Its tables depend only on the geometry and the mask.
-  static constexpr int kFlow = -4;
+  // ---- dependency-flow kernel (FP32: variant kFlow or kFlow12; mixed:
+  // mvariant kFlow) ---------------------------------------------------------------
+  // Its tables depend only on the geometry, the mask and the depth.
+  static constexpr int kFlow = -4;    // depth 16 ("p16w8k16d")
+  static constexpr int kFlow12 = -5;  // depth 12 ("p16w8k12d"), FP32 Jacobi only
+  static bool is_flow(int v) { return v == kFlow || v == kFlow12; }
+  // Depth of the flow launches the current settings make.
+  int flow_k() const { return precision == FPIE_FP32 && variant == kFlow12 ? 12 : flow_depth(); }
   uint8_t* ft_flags = nullptr;  // tile flags for the flow tiling
+  uint8_t* code = nullptr;      // masked / pinned bits per pixel (launch_grid_code)
   int* ft_list = nullptr;       // active-tile list (count + indices)
   int* flow_inv = nullptr;      // tile -> active-list index
   void* flow_rec = nullptr;     // per active tile: index, flag, neighbourhood
   int* flow_done = nullptr;     // levels finished per (active tile, channel)
   int flow_cap = 0;             // tiles the arrays hold
   int ft_tiles_x = 0, ft_tiles = 0;
+  int ft_k = 0;  // depth the tables were built for
   bool ft_ok = false;
   int flow_grid = 0;
 
@@ -183,10 +190,10 @@ struct GridSolverImpl : Solver {
   void run_flow(int iters) {
     ensure_flow_tables();
     FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
-    launch_flow(G, mask, g, x[0], x[1], cur, ft_list, flow_rec, flow_done, ft_tiles_x, ft_tiles,
-                iters, d_wait_err, spin_limit, flow_grid, stream, red_black);
+    launch_flow(G, mask, code, g, x[0], x[1], cur, ft_list, flow_rec, flow_done, ft_tiles_x,
+                ft_tiles, iters, d_wait_err, spin_limit, flow_grid, stream, red_black, ft_k);
     post_launch(this);
-    const int per_level = red_black ? flow_rb_depth() : flow_depth();
+    const int per_level = red_black ? flow_rb_depth() : ft_k;
     const int levels = (iters + per_level - 1) / per_level;
     if (levels & 1) cur ^= 1;
   }
@@ -270,6 +277,7 @@ struct GridSolverImpl : Solver {
     cudaFree(x[1]);
     cudaFree(g);
     cudaFree(mask);
+    cudaFree(code);
     cudaFree(d_img);
     cudaFree(d_part);
     cudaFree(d_err);
@@ -299,6 +307,7 @@ struct GridSolverImpl : Solver {
     tma_list_cap = 0;
     x[0] = x[1] = g = nullptr;
     mask = nullptr;
+    code = nullptr;
     d_img = nullptr;
     d_part = nullptr;
     d_err = nullptr;
@@ -330,6 +339,7 @@ struct GridSolverImpl : Solver {
     FPIE_CUDA(cudaMalloc(&x[1], 3 * pb));
     FPIE_CUDA(cudaMalloc(&g, 3 * pb));
     FPIE_CUDA(cudaMalloc(&mask, (size_t)G.plane));
+    FPIE_CUDA(cudaMalloc(&code, (size_t)G.plane));
     FPIE_CUDA(cudaMalloc(&d_img, (size_t)n * m * 3));
     FPIE_CUDA(cudaMalloc(&d_part, (size_t)L.nparts * 3 * sizeof(double)));
     FPIE_CUDA(cudaMalloc(&d_err, 3 * sizeof(float)));
@@ -501,12 +511,12 @@ struct GridSolverImpl : Solver {
 
   int depth() const {
     if (variant == kTma) return tma_depth();
-    if (variant == kFlow) return flow_depth();
+    if (is_flow(variant)) return flow_k();
     return variant < 0 ? 1 : tb_variants()[variant].depth;
   }
 
   void ensure_flags() {
-    if (variant == kFlow) {
+    if (is_flow(variant)) {
       ensure_flow_tables();
       return;
     }
@@ -557,8 +567,9 @@ struct GridSolverImpl : Solver {
 
   // Flags, active-tile list, records and counters of the flow tiling.
   void ensure_flow_tables() {
-    if (ft_ok) return;
-    const int th = flow_tile_h(), tw = flow_tile_w(), kd = flow_depth();
+    const int kd = flow_k();
+    if (ft_ok && ft_k == kd) return;
+    const int th = flow_tile_h(kd), tw = flow_tile_w(kd);
     ft_tiles_x = (G.m + tw - 1) / tw;
     ft_tiles = ft_tiles_x * ((G.n + th - 1) / th);
     if (ft_tiles > flow_cap) {
@@ -583,8 +594,12 @@ struct GridSolverImpl : Solver {
     post_launch(this);
     launch_tma_list(ft_flags, ft_tiles, ft_list, stream);
     post_launch(this);
-    launch_flow_tables(ft_list, ft_flags, ft_tiles_x, ft_tiles, flow_inv, flow_rec, stream);
+    launch_grid_code(G, mask, code, stream);
     post_launch(this);
+    launch_flow_tables(G, code, kd, ft_list, ft_flags, ft_tiles_x, ft_tiles, flow_inv, flow_rec,
+                       stream);
+    post_launch(this, 3);
+    ft_k = kd;
     ft_ok = true;
   }
 
@@ -677,7 +692,7 @@ struct GridSolverImpl : Solver {
       }
     }
     // Candidates: four packed temporally blocked variants, then the flow
-    // kernel below.  sweep1 (one sweep per launch, the baseline) and the TMA
+    // kernel below (two depths).  sweep1 (one sweep per launch, the baseline) and the TMA
     // kernel stay available by name but were never the fastest on a
     // measured shape; timing them would only lengthen the first step.
     static const char* const kTuned[] = {"p16w8k16", "p8w16k16", "p16w8k8", "p8w8k8"};
@@ -716,9 +731,12 @@ struct GridSolverImpl : Solver {
     }
     // The dependency-flow kernel runs a whole step per launch; timed on 4
     // chunks per launch so that its start and end (one level each) weigh as
-    // little as in a real step.
-    if (iters - used >= (kTuneReps + 1) * 4 * kChunk) {
-      select_variant(kFlow);
+    // little as in a real step.  Both depths for Jacobi sweeps: which tiling
+    // covers the grid with less work depends on its extents.
+    for (int fv : {kFlow, kFlow12}) {
+      if (fv == kFlow12 && red_black) continue;
+      if (iters - used < (kTuneReps + 1) * 4 * kChunk) break;
+      select_variant(fv);
       run_flow(4 * kChunk);
       used += 4 * kChunk;
       for (int r = 0; r < kTuneReps; ++r) {
@@ -731,7 +749,7 @@ struct GridSolverImpl : Solver {
         used += 4 * kChunk;
         if (ms / 4 < best_ms) {
           best_ms = ms / 4;
-          best = kFlow;
+          best = fv;
         }
       }
       check_waits();
@@ -753,7 +771,7 @@ struct GridSolverImpl : Solver {
       return;
     }
     if (!tuned && !pinned) iters -= autotune(iters);
-    if (variant == kFlow) {
+    if (is_flow(variant)) {
       if (iters > 0) run_flow(iters);
       return;
     }
@@ -1049,6 +1067,7 @@ struct GridSolverImpl : Solver {
     if (name == "sweep1") v = -1;
     if (name == "p16w8k16t") v = kTma;
     if (name == "p16w8k16d") v = kFlow;
+    if (name == "p16w8k12d") v = kFlow12;
     for (size_t k = 0; k < tb_variants().size(); ++k)
       if (name == tb_variants()[k].name && !tb_variants()[k].red_black) v = (int)k;
     FPIE_REQUIRE(v != -100, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
@@ -1062,6 +1081,7 @@ struct GridSolverImpl : Solver {
     if (variant == kTma) return std::string("p16w8k16t");
     if (variant == kFlow && red_black) return std::string(tb_variants()[red_black_variant()].name) + "d";
     if (variant == kFlow) return std::string("p16w8k16d");
+    if (variant == kFlow12) return std::string("p16w8k12d");
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }
 

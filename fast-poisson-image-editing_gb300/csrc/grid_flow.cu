@@ -1,15 +1,17 @@
-// Dependency-flow grid sweep ("p16w8k16d"): a whole step in one launch.
+// Dependency-flow grid sweep ("p16w8k16d", "p16w8k12d"): a whole step in
+// one launch.
 //
-// The sweeps are cut into levels of up to 16 (the packed variant
+// The sweeps are cut into levels of up to K = 16 (the packed variant
 // p16w8k16's temporal depth: 96x96 tiles in 128x128 register-resident
-// regions, same arithmetic, bit-identical results).  A work item is one
+// regions, same arithmetic, bit-identical results) or K = 12 (104x104
+// tiles in the same regions).  A work item is one
 // (level, active tile, channel); items are numbered level-major and CTA b
 // of a cooperative launch takes items b, b + gridDim.x, ...  Item
 // (z, tile, c) reads buffer (p + z) & 1 over its region and writes the tile
 // interior to buffer (p + z + 1) & 1.  It may start once every active tile
 // of its 3x3 neighbourhood (same channel, itself included) has finished
 // level z - 1, which covers both hazards on the ping-pong buffers:
-//   - read after write: the region (tile + 16-pixel apron) lies inside the
+//   - read after write: the region (tile + K-pixel apron) lies inside the
 //     neighbourhood, whose level z - 1 outputs are then complete;
 //   - write after read: the buffer being written was read at level z - 1
 //     only by items of the neighbourhood, which are then finished.
@@ -46,21 +48,44 @@ namespace fpie {
 
 namespace {
 
-constexpr int kR = 16, kW = 8, kK = 16;
-constexpr int kTH = kW * kR - 2 * kK;  // 96
-constexpr int kTW = 128 - 2 * kK;      // 96
+constexpr int kR = 16, kW = 8;
+// Temporal depth K (sweeps per level, and the apron): tiles of
+// (8 * 16 - 2K) x (128 - 2K) in 128 x 128 regions.  K = 16 (96 x 96 tiles)
+// runs every form; K = 12 (104 x 104 tiles, FP32 Jacobi only) covers some
+// grids with fewer tiles -- an 802-pixel side takes 8 of them instead of 9,
+// which cuts the region work per sweep by a fifth.
+constexpr int kK = 16;
+template <int K>
+struct FlowTile {
+  static_assert(K % 4 == 0 && K <= kPad, "the apron must keep float4 columns aligned");
+  static constexpr int H = kW * kR - 2 * K;
+  static constexpr int W = 128 - 2 * K;
+};
 
 // Per active tile: {tile, flag, nb[0..8]} with nb = 3 x (active-list index)
 // of each tile of the 3x3 neighbourhood (row-major, itself at 4), -1 where
-// there is no active tile; padded to 12 ints (three int4 loads).
+// there is no active tile; padded to 12 ints (three int4 loads).  flag: 2 =
+// region fully masked (no selects); else the region's pinned-boundary
+// sweep body for FP32 Jacobi sweeps (kBody*; the mixed and red-black forms
+// take their select path for any flag but 2).
 struct FlowRec {
   int tile, flag, nb[9], pad;
 };
 static_assert(sizeof(FlowRec) == 48, "three int4");
 
+// Sweep bodies of regions holding unmasked pixels (FlowRec.flag), chosen
+// once per mask by flow_body_kernel from where the region's pinned pixels
+// lie: every one in the same column group of the lanes (a vertical edge),
+// in at most two pair rows of every warp (horizontal edges), or anywhere
+// (kBodyAll: the select on every unmasked pixel, which measured faster
+// than selecting the pinned ones in every group and storing around the
+// free ones).
+constexpr int kBodyAll = 3, kBodyRows = 4, kBodyCol0 = 5;  // kBodyCol0 + j: column group j
+
 struct FlowArgs {
   GridGeom G;
   const uint8_t* mask;
+  const uint8_t* code;   // FP32 Jacobi: per pixel bit 0 = masked, bit 1 = pinned
   const float* g;
   float* x[2];
   void* e[2];            // mixed forms: the correction planes (FP16 / BF16)
@@ -102,17 +127,21 @@ __device__ __forceinline__ bool counters_reach(const int (&v)[9], int level) {
 
 // Thread 0: waits until the counters in v (loaded earlier, possibly stale --
 // counters only grow) all reach `level`, reloading them together each round.
+// A round is one L2 round trip: the error flag is loaded with the counters,
+// not before them, and the first rounds poll again at once (a neighbour
+// about to finish is the common case); later rounds back off 64 ns.
 // False if the wait gave up or another CTA did.
 __device__ __forceinline__ bool wait_counters(const FlowArgs& A, const FlowRec& R, int c,
                                               int level, int (&v)[9]) {
   for (long long spins = 0; !counters_reach(v, level); ++spins) {
-    if (*(volatile int*)A.error) return false;
     if (spins >= A.spin_limit) {
       atomicExch(A.error, 1);
       return false;
     }
-    __nanosleep(64);
+    if (spins >= 8) __nanosleep(64);
+    const int err = *(volatile int*)A.error;
     load_counters(A, R, c, v);
+    if (err) return false;
   }
   return true;
 }
@@ -120,19 +149,76 @@ __device__ __forceinline__ bool wait_counters(const FlowArgs& A, const FlowRec& 
 // One item, out of line: inlined into the item loop, the compiler's register
 // assignment needs several times the register moves per sweep of the same
 // code in the launch-per-tile kernel (measured by instruction counters).
-template <bool FULL>
+// One FP32 Jacobi item of a fully masked region (FULL: no selects) or of a
+// region whose unmasked pixels all keep their values by a select (!FULL).
+template <int K, bool FULL>
 __device__ __noinline__ void flow_item(const FlowArgs& A, int tile, int c, int z,
                                        float4 (&edge)[2][2][kW][32], int lane, int w) {
   const GridGeom& G = A.G;
   const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
-  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long base = G.at(ty * FlowTile<K>::H - K + w * kR, tx * FlowTile<K>::W - K + 4 * lane);
   const long long co = c * G.plane;
   const int pin = (A.parity + z) & 1;
-  const int ks = min(kK, A.sweeps - z * kK);
+  const int ks = min(K, A.sweeps - z * K);
   // CG: the state is read through L2, since other CTAs wrote it during
   // this launch.
-  tbp_body<kR, kW, kK, FULL, float, false, true>(G, A.mask, A.g + co, A.x[pin] + co,
-                                                 A.x[pin ^ 1] + co, base, ks, lane, w, edge);
+  tbp_body<kR, kW, K, FULL, float, false, true>(G, A.mask, A.g + co, A.x[pin] + co,
+                                                A.x[pin ^ 1] + co, base, ks, lane, w, edge);
+}
+
+// One FP32 Jacobi item of a region whose pinned pixels lie in one column
+// group or in few pair rows, by its body (FlowRec.flag): the pinned-boundary
+// sweeps (code plane, free pixels not stored).  The five bodies share one
+// function (out-of-line bodies of their own measured slower); the select on
+// every unmasked pixel has its own (flow_item), where it runs as fast as
+// alone.
+template <int K>
+__device__ __noinline__ void flow_pin_item(const FlowArgs& A, int flag, int tile, int c, int z,
+                                           float4 (&edge)[2][2][kW][32], int lane, int w) {
+  const GridGeom& G = A.G;
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const long long base = G.at(ty * FlowTile<K>::H - K + w * kR, tx * FlowTile<K>::W - K + 4 * lane);
+  const long long co = c * G.plane;
+  const int pin = (A.parity + z) & 1;
+  const int ks = min(K, A.sweeps - z * K);
+  const float* gc = A.g + co;
+  const float* xi = A.x[pin] + co;
+  float* xo = A.x[pin ^ 1] + co;
+  switch (flag) {
+    case kBodyRows:
+      tbp_body<kR, kW, K, false, float, false, true, false, false, kRowSel>(G, A.code, gc, xi, xo,
+                                                                         base, ks, lane, w, edge);
+      break;
+    case kBodyCol0:
+      tbp_body<kR, kW, K, false, float, false, true, false, false, 1>(G, A.code, gc, xi, xo, base,
+                                                                   ks, lane, w, edge);
+      break;
+    case kBodyCol0 + 1:
+      tbp_body<kR, kW, K, false, float, false, true, false, false, 2>(G, A.code, gc, xi, xo, base,
+                                                                   ks, lane, w, edge);
+      break;
+    case kBodyCol0 + 2:
+      tbp_body<kR, kW, K, false, float, false, true, false, false, 4>(G, A.code, gc, xi, xo, base,
+                                                                   ks, lane, w, edge);
+      break;
+    default:
+      tbp_body<kR, kW, K, false, float, false, true, false, false, 8>(G, A.code, gc, xi, xo, base,
+                                                                   ks, lane, w, edge);
+      break;
+  }
+}
+
+// The FP32 Jacobi item of a region with body `flag` (FlowRec).
+template <int K>
+__device__ __forceinline__ void flow_jacobi_item(const FlowArgs& A, int flag, int tile, int c,
+                                                 int z, float4 (&edge)[2][2][kW][32], int lane,
+                                                 int w) {
+  if (flag == 2)
+    flow_item<K, true>(A, tile, c, z, edge, lane, w);
+  else if (flag == kBodyAll)
+    flow_item<K, false>(A, tile, c, z, edge, lane, w);
+  else
+    flow_pin_item<K>(A, flag, tile, c, z, edge, lane, w);
 }
 
 // One item of the red-black order (the EquSolver's grid placement): kK / 2
@@ -142,7 +228,7 @@ __device__ __noinline__ void flow_rb_item(const FlowArgs& A, int tile, int c, in
                                           float4 (&edge)[2][2][kW][32], int lane, int w) {
   const GridGeom& G = A.G;
   const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
-  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long base = G.at(ty * FlowTile<kK>::H - kK + w * kR, tx * FlowTile<kK>::W - kK + 4 * lane);
   const long long co = c * G.plane;
   const int pin = (A.parity + z) & 1;
   const int ks = min(kK / 2, A.sweeps - z * (kK / 2));
@@ -160,7 +246,7 @@ __device__ __noinline__ void flow_fold_item(const FlowArgs& A, int tile, int c, 
                                             float4 (&edge)[2][2][kW][32], int lane, int w) {
   const GridGeom& G = A.G;
   const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
-  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long base = G.at(ty * FlowTile<kK>::H - kK + w * kR, tx * FlowTile<kK>::W - kK + 4 * lane);
   const long long co = c * G.plane;
   const float* gc = A.g + co;
   TS* e0 = static_cast<TS*>(A.e[0]);
@@ -182,7 +268,7 @@ __device__ __noinline__ void flow_inner_item(const FlowArgs& A, int tile, int c,
                                              float4 (&edge)[2][2][kW][32], int lane, int w) {
   const GridGeom& G = A.G;
   const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
-  const long long base = G.at(ty * kTH - kK + w * kR, tx * kTW - kK + 4 * lane);
+  const long long base = G.at(ty * FlowTile<kK>::H - kK + w * kR, tx * FlowTile<kK>::W - kK + 4 * lane);
   const long long co = c * G.plane;
   TS* e0 = static_cast<TS*>(A.e[0]);
   TS* e1 = static_cast<TS*>(A.e[1]);
@@ -202,8 +288,8 @@ __device__ __noinline__ void flow_flush_item(const FlowArgs& A, int tile, int c,
   TS* e1 = static_cast<TS*>(A.e[1]);
   const int xp = (A.parity + cycle - 1) & 1;
   const TS* elast = (((nlast - 1) & 1) ? e1 : e0) + co;
-  refine_tile<TS>(G, A.mask, A.g + co, A.x[xp] + co, elast, A.x[xp ^ 1] + co, nullptr, ty * kTH,
-                  tx * kTW, kTH, kTW);
+  refine_tile<TS>(G, A.mask, A.g + co, A.x[xp] + co, elast, A.x[xp ^ 1] + co, nullptr, ty * FlowTile<kK>::H,
+                  tx * FlowTile<kK>::W, FlowTile<kK>::H, FlowTile<kK>::W);
 }
 
 // Thread 0 keeps the next item's record and counters, loaded right after
@@ -211,15 +297,17 @@ __device__ __noinline__ void flow_flush_item(const FlowArgs& A, int tile, int c,
 // fence and barrier; the other threads get tile and flag through shared
 // memory.
 // TS = float: the FP32 sweeps; __half / __nv_bfloat16: the mixed forms.
-template <typename TS>
+// K: the temporal depth (the mixed and red-black forms run at kK only).
+template <typename TS, int K>
 __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
   constexpr bool MIXED = !std::is_same<TS, float>::value;
+  static_assert(K == kK || !MIXED, "the mixed forms' cycles are 64 sweeps of kK-sweep levels");
   __shared__ float4 edge[2][2][kW][32];
   __shared__ int s_stop, s_tile, s_flag;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int per = 3 * A.list[-1];
-  const int per_level = A.red_black ? kK / 2 : kK;
-  const int levels = MIXED ? mixed_levels(A.sweeps, kK) : (A.sweeps + per_level - 1) / per_level;
+  const int per_level = A.red_black ? K / 2 : K;
+  const int levels = MIXED ? mixed_levels(A.sweeps, K) : (A.sweeps + per_level - 1) / per_level;
   const long long total = (long long)levels * per;
   FlowRec R{};
   int v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -244,7 +332,7 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
     if (s_stop) break;
     const int tile = s_tile;
     if constexpr (MIXED) {
-      const MixedLevel L = mixed_level(z, A.sweeps, kK);
+      const MixedLevel L = mixed_level(z, A.sweeps, K);
       if (L.type == 0) {
         if (s_flag == 2)
           flow_fold_item<true, TS>(A, tile, c, L.cycle, L.k, edge, lane, w);
@@ -258,15 +346,17 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
       } else {
         flow_flush_item<TS>(A, tile, c, L.cycle, L.nlast);
       }
-    } else if (A.red_black) {
-      if (s_flag == 2)
-        flow_rb_item<true>(A, tile, c, z, edge, lane, w);
-      else
-        flow_rb_item<false>(A, tile, c, z, edge, lane, w);
-    } else if (s_flag == 2) {
-      flow_item<true>(A, tile, c, z, edge, lane, w);
+    } else if constexpr (K == kK) {
+      if (A.red_black) {
+        if (s_flag == 2)
+          flow_rb_item<true>(A, tile, c, z, edge, lane, w);
+        else
+          flow_rb_item<false>(A, tile, c, z, edge, lane, w);
+      } else {
+        flow_jacobi_item<K>(A, s_flag, tile, c, z, edge, lane, w);
+      }
     } else {
-      flow_item<false>(A, tile, c, z, edge, lane, w);
+      flow_jacobi_item<K>(A, s_flag, tile, c, z, edge, lane, w);
     }
     const long long next = idx + gridDim.x;
     if (threadIdx.x == 0 && next < total) {
@@ -284,6 +374,65 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
 }
 
 // inv[t] = index of tile t in the active list, -1 for inactive tiles.
+__global__ void grid_code_kernel(GridGeom G, const uint8_t* __restrict__ mask,
+                                 uint8_t* __restrict__ code) {
+  const long long n = G.plane;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int row = (int)(p / G.pitch), col = (int)(p - (long long)row * G.pitch);
+    uint8_t c = 1;
+    if (!mask[p]) {
+      const bool nb = (row > 0 && mask[p - G.pitch]) || (row < G.rows - 1 && mask[p + G.pitch]) ||
+                      (col > 0 && mask[p - 1]) || (col < G.pitch - 1 && mask[p + 1]);
+      c = nb ? 2 : 0;
+    }
+    code[p] = c;
+  }
+}
+
+// One block per active tile (blocks past the active count return): the
+// sweep body of its region (kBody*) from the code plane, for regions with
+// unmasked pixels (tile flag 1).  Warps whose strip holds no masked pixel
+// idle in the sweeps and do not count.
+__global__ void flow_body_kernel(GridGeom G, const uint8_t* __restrict__ code,
+                                 const int* __restrict__ list, int tiles_x, int th, int tw, int k,
+                                 FlowRec* __restrict__ rec) {
+  __shared__ unsigned s_masked[kW], s_col[kW], s_rows[kW];
+  const int a = blockIdx.x;
+  if (a >= list[-1] || rec[a].flag == 2) return;  // uniform per block
+  if (threadIdx.x < kW) s_masked[threadIdx.x] = s_col[threadIdx.x] = s_rows[threadIdx.x] = 0;
+  __syncthreads();
+  const int tile = list[a], ty = tile / tiles_x, tx = tile - ty * tiles_x;
+  const int r0 = ty * th - k, c0 = tx * tw - k;
+  for (int q = threadIdx.x; q < kW * kR * 128; q += blockDim.x) {
+    const int i = q >> 7, j = q & 127;  // region row, column
+    const uint8_t cv = code[G.at(r0 + i, c0 + j)];
+    const int w = i / kR, pr = (i % kR) % (kR / 2);
+    if (cv & 1) s_masked[w] = 1;
+    if (cv & 2) {
+      atomicOr(&s_col[w], 1u << (j & 3));
+      atomicOr(&s_rows[w], 1u << pr);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned col = 0;
+    bool wide = false;
+    for (int w = 0; w < kW; ++w)
+      if (s_masked[w]) {
+        col |= s_col[w];
+        wide = wide || __popc(s_rows[w]) > 2;
+      }
+    int body = kBodyAll;
+    if (col == 0 || col == 1) body = kBodyCol0;
+    else if (col == 2) body = kBodyCol0 + 1;
+    else if (col == 4) body = kBodyCol0 + 2;
+    else if (col == 8) body = kBodyCol0 + 3;
+    else if (!wide) body = kBodyRows;
+    rec[a].flag = body;
+  }
+}
+
 __global__ void flow_inv_kernel(const int* __restrict__ list, int tiles, int* __restrict__ inv) {
   const int n = list[-1];
   for (int t = threadIdx.x; t < tiles; t += blockDim.x) inv[t] = -1;
@@ -312,8 +461,9 @@ __global__ void flow_rec_kernel(const int* __restrict__ list, const int* __restr
 
 }  // namespace
 
-int flow_tile_h() { return kTH; }
-int flow_tile_w() { return kTW; }
+bool flow_depth_ok(int depth) { return depth == 16 || depth == 12; }
+int flow_tile_h(int depth) { return depth == 12 ? FlowTile<12>::H : FlowTile<kK>::H; }
+int flow_tile_w(int depth) { return depth == 12 ? FlowTile<12>::W : FlowTile<kK>::W; }
 int flow_depth() { return kK; }
 int flow_rb_depth() { return kK / 2; }
 
@@ -327,8 +477,10 @@ int flow_ctas() {
     return cached[dev].load(std::memory_order_relaxed);
   FPIE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int m = 1 << 30;
-  const void* ks[3] = {(const void*)grid_flow_kernel<float>, (const void*)grid_flow_kernel<__half>,
-                       (const void*)grid_flow_kernel<__nv_bfloat16>};
+  const void* ks[4] = {(const void*)grid_flow_kernel<float, kK>,
+                       (const void*)grid_flow_kernel<float, 12>,
+                       (const void*)grid_flow_kernel<__half, kK>,
+                       (const void*)grid_flow_kernel<__nv_bfloat16, kK>};
   for (const void* k : ks) {
     FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kW * 32, 0));
     m = std::min(m, per_sm);
@@ -338,29 +490,41 @@ int flow_ctas() {
   return sms * m;
 }
 
-void launch_flow_tables(const int* list, const uint8_t* flags, int tiles_x, int tiles, int* inv,
-                        void* rec, cudaStream_t st) {
+void launch_flow_tables(const GridGeom& G, const uint8_t* code, int depth, const int* list,
+                        const uint8_t* flags, int tiles_x, int tiles, int* inv, void* rec,
+                        cudaStream_t st) {
   flow_inv_kernel<<<1, 1024, 0, st>>>(list + 1, tiles, inv);
   flow_rec_kernel<<<(tiles + 255) / 256, 256, 0, st>>>(list + 1, inv, flags, tiles_x,
                                                        tiles / tiles_x,
                                                        static_cast<FlowRec*>(rec));
+  flow_body_kernel<<<tiles, 256, 0, st>>>(G, code, list + 1, tiles_x, flow_tile_h(depth),
+                                          flow_tile_w(depth), depth, static_cast<FlowRec*>(rec));
 }
 
 size_t flow_rec_bytes() { return sizeof(FlowRec); }
 
-void launch_flow(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
-                 int parity, const int* list, const void* rec, int* done, int tiles_x, int tiles,
-                 int sweeps, int* error, long long spin_limit, int ctas, cudaStream_t st,
-                 bool red_black) {
+void launch_grid_code(const GridGeom& G, const uint8_t* mask, uint8_t* code, cudaStream_t st) {
+  grid_code_kernel<<<stride_blocks(G.plane, 256, 4), 256, 0, st>>>(G, mask, code);
+}
+
+void launch_flow(const GridGeom& G, const uint8_t* mask, const uint8_t* code, const float* g,
+                 float* x0, float* x1, int parity, const int* list, const void* rec, int* done,
+                 int tiles_x, int tiles, int sweeps, int* error, long long spin_limit, int ctas,
+                 cudaStream_t st,
+                 bool red_black, int depth) {
   FPIE_REQUIRE(sweeps >= 1, FPIE_ERR_ARG, "flow sweep kernel: at least one sweep");
+  FPIE_REQUIRE(depth == kK || (depth == 12 && !red_black), FPIE_ERR_ARG,
+               "flow sweep kernel: depth 16, or 12 for Jacobi sweeps");
+  FPIE_REQUIRE(red_black || code, FPIE_ERR_STATE, "flow sweep kernel: no code plane");
   FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
                "flow sweep kernel: bad tiling");
-  FlowArgs a{G, mask, g, {x0, x1}, {nullptr, nullptr}, nullptr, list + 1,
+  FlowArgs a{G, mask, code, g, {x0, x1}, {nullptr, nullptr}, nullptr, list + 1,
              static_cast<const FlowRec*>(rec), done, error, tiles_x, sweeps, parity & 1,
              spin_limit, red_black ? 1 : 0};
   void* args[] = {&a};
-  FPIE_CUDA(cudaLaunchCooperativeKernel((const void*)grid_flow_kernel<float>, dim3(ctas),
-                                        dim3(kW * 32), args, 0, st));
+  const void* k = depth == 12 ? (const void*)grid_flow_kernel<float, 12>
+                              : (const void*)grid_flow_kernel<float, kK>;
+  FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, 0, st));
 }
 
 void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
@@ -370,11 +534,11 @@ void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, f
   FPIE_REQUIRE(sweeps >= 1, FPIE_ERR_ARG, "flow sweep kernel: at least one sweep");
   FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
                "flow sweep kernel: bad tiling");
-  FlowArgs a{G, mask, g, {x0, x1}, {e0, e1}, r, list + 1, static_cast<const FlowRec*>(rec), done,
+  FlowArgs a{G, mask, nullptr, g, {x0, x1}, {e0, e1}, r, list + 1, static_cast<const FlowRec*>(rec), done,
              error, tiles_x, sweeps, parity & 1, spin_limit, 0};
   void* args[] = {&a};
-  const void* k = bf16 ? (const void*)grid_flow_kernel<__nv_bfloat16>
-                       : (const void*)grid_flow_kernel<__half>;
+  const void* k = bf16 ? (const void*)grid_flow_kernel<__nv_bfloat16, kK>
+                       : (const void*)grid_flow_kernel<__half, kK>;
   FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, 0, st));
 }
 

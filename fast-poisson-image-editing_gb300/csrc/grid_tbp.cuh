@@ -5,6 +5,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace fpie {
@@ -221,6 +223,171 @@ __device__ __forceinline__ void tbp_sweeps(float2 (&P)[R / 2][4], const float2 (
   if (s < ksweeps) tbp_sweep<R, W, FULL, GS, true>(P, Gp, mk, 0, lane, w, edge, sg);
 }
 
+// ---- pinned-boundary sweeps (FP32 Jacobi on regions holding unmasked pixels)
+// The words in mk are code bytes: bit 0 = masked, bit 1 = pinned, i.e.
+// unmasked with a masked 4-neighbour.  Only pinned pixels must keep their
+// values: every 4-neighbour of a masked pixel is masked or pinned, so what
+// the other unmasked ("free") pixels compute never reaches a masked pixel,
+// and they are not stored (store_kept).  Selects are then needed only where
+// pinned pixels lie.  These are copies of tbp_update / tbp_sweep with
+// those selects (the select path above keeps its own code unchanged).
+
+// SEL: select in the column groups j of bit j, or (kRowSel) in every group
+// of the pair rows i of the warp-uniform mask rsel (bit i).
+constexpr int kRowSel = 16;
+
+template <int R, int SEL>
+__device__ __forceinline__ void tbp_update_pin(const float2 (&cur)[4], const float2 (&up)[4],
+                                               const float2 (&dn)[4], const float2 (&gv)[4],
+                                               const uint32_t (&mk)[R], int i, float2 (&o)[4],
+                                               uint32_t rsel) {
+  constexpr int H = R / 2;
+  const float2 q = make_float2(0.25f, 0.25f);
+  const float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cur[3].x, 1),
+                                __shfl_up_sync(0xffffffffu, cur[3].y, 1));
+  const float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cur[0].x, 1),
+                                __shfl_down_sync(0xffffffffu, cur[0].y, 1));
+  float2 t[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(gv[j], up[j]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], dn[j]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], j > 0 ? cur[j - 1] : lf);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) t[j] = __fadd2_rn(t[j], j < 3 ? cur[j + 1] : rt);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) o[j] = __fmul2_rn(t[j], q);
+  if (SEL == kRowSel) {
+    if ((rsel >> i) & 1u) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) o[j] = pick2(mk[i], mk[i + H], 0x02u << (8 * j), cur[j], o[j]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (SEL & (1 << j)) o[j] = pick2(mk[i], mk[i + H], 0x02u << (8 * j), cur[j], o[j]);
+  }
+}
+
+template <int R, int W, int SEL, bool FWD>
+__device__ __forceinline__ void tbp_sweep_pin(float2 (&P)[R / 2][4], const float2 (&Gp)[R / 2][4],
+                                              const uint32_t (&mk)[R], int par, int lane, int w,
+                                              float4 (&edge)[2][2][W][32], uint32_t rsel) {
+  constexpr int H = R / 2;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  edge[par][0][w][lane] = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+  edge[par][1][w][lane] = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+  __syncthreads();
+  const float4 above = w > 0 ? edge[par][1][w - 1][lane] : zero;
+  const float4 below = w < W - 1 ? edge[par][0][w + 1][lane] : zero;
+  const float2 ufirst[4] = {make_float2(above.x, P[H - 1][0].x), make_float2(above.y, P[H - 1][1].x),
+                            make_float2(above.z, P[H - 1][2].x), make_float2(above.w, P[H - 1][3].x)};
+  const float2 dlast[4] = {make_float2(P[0][0].y, below.x), make_float2(P[0][1].y, below.y),
+                           make_float2(P[0][2].y, below.z), make_float2(P[0][3].y, below.w)};
+  if (FWD) {
+    float2 up[4] = {ufirst[0], ufirst[1], ufirst[2], ufirst[3]};
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      const float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
+      float2 dn[4], o[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dn[j] = i < H - 1 ? P[i + 1][j] : dlast[j];
+      tbp_update_pin<R, SEL>(cur, up, dn, Gp[i], mk, i, o, rsel);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        up[j] = cur[j];
+        P[i][j] = o[j];
+      }
+    }
+  } else {
+    float2 dn[4] = {dlast[0], dlast[1], dlast[2], dlast[3]};
+#pragma unroll
+    for (int i = H - 1; i >= 0; --i) {
+      const float2 cur[4] = {P[i][0], P[i][1], P[i][2], P[i][3]};
+      float2 up[4], o[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) up[j] = i > 0 ? P[i - 1][j] : ufirst[j];
+      tbp_update_pin<R, SEL>(cur, up, dn, Gp[i], mk, i, o, rsel);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        dn[j] = cur[j];
+        P[i][j] = o[j];
+      }
+    }
+  }
+}
+
+// ksweeps pinned-boundary sweeps of the strip in P (forward/backward pairs,
+// one barrier per sweep, like tbp_sweeps).  The caller picks SEL per region,
+// so that every warp of the CTA runs the same sweep code.  A warp whose
+// strip holds no masked pixel only publishes its edges and takes part in
+// the barriers; false then (nothing of it needs storing).
+template <int R, int W, int SEL>
+__device__ __forceinline__ bool tbp_sweeps_pin(float2 (&P)[R / 2][4], const float2 (&Gp)[R / 2][4],
+                                               const uint32_t (&mk)[R], int ksweeps, int lane, int w,
+                                               float4 (&edge)[2][2][W][32]) {
+  constexpr int H = R / 2;
+  uint32_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) acc |= mk[i];
+  if (__all_sync(0xffffffffu, (acc & 0x01010101u) == 0u)) {
+    const float4 top = make_float4(P[0][0].x, P[0][1].x, P[0][2].x, P[0][3].x);
+    const float4 bot = make_float4(P[H - 1][0].y, P[H - 1][1].y, P[H - 1][2].y, P[H - 1][3].y);
+    for (int s = 0; s < ksweeps; ++s) {
+      edge[s & 1][0][w][lane] = top;
+      edge[s & 1][1][w][lane] = bot;
+      __syncthreads();
+    }
+    return false;
+  }
+  uint32_t rsel = 0;
+  if (SEL == kRowSel) {
+#pragma unroll
+    for (int i = 0; i < H; ++i)
+      if ((mk[i] | mk[i + H]) & 0x02020202u) rsel |= 1u << i;
+    rsel = __reduce_or_sync(0xffffffffu, rsel);
+  }
+  int s = 0;
+  for (; s + 2 <= ksweeps; s += 2) {
+    tbp_sweep_pin<R, W, SEL, true>(P, Gp, mk, 0, lane, w, edge, rsel);
+    tbp_sweep_pin<R, W, SEL, false>(P, Gp, mk, 1, lane, w, edge, rsel);
+  }
+  if (s < ksweeps) tbp_sweep_pin<R, W, SEL, true>(P, Gp, mk, 0, lane, w, edge, rsel);
+  return true;
+}
+
+// Stores the 4 FP32 state values at p whose pixels are not free (code
+// bytes in `word`: masked, or pinned -- a pinned value never changed, so
+// storing it is harmless): one vector store when all four are, else
+// predicated scalar stores, without branches (a divergent branch per row
+// costs more than the stores).
+__device__ __forceinline__ void store_kept(float* p, float4 v, uint32_t word) {
+  const uint32_t m = (word | (word >> 1)) & 0x01010101u;
+  asm volatile(
+      "{\n\t"
+      ".reg .pred pv, p0, p1, p2, p3;\n\t"
+      ".reg .b32 t;\n\t"
+      "setp.eq.u32 pv, %5, 16843009;\n\t"
+      "@pv st.global.v4.f32 [%0], {%1, %2, %3, %4};\n\t"
+      "and.b32 t, %5, 1;\n\t"
+      "setp.ne.and.u32 p0, t, 0, !pv;\n\t"
+      "and.b32 t, %5, 256;\n\t"
+      "setp.ne.and.u32 p1, t, 0, !pv;\n\t"
+      "and.b32 t, %5, 65536;\n\t"
+      "setp.ne.and.u32 p2, t, 0, !pv;\n\t"
+      "and.b32 t, %5, 16777216;\n\t"
+      "setp.ne.and.u32 p3, t, 0, !pv;\n\t"
+      "@p0 st.global.f32 [%0], %1;\n\t"
+      "@p1 st.global.f32 [%0+4], %2;\n\t"
+      "@p2 st.global.f32 [%0+8], %3;\n\t"
+      "@p3 st.global.f32 [%0+12], %4;\n\t"
+      "}"
+      :
+      : "l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(m)
+      : "memory");
+}
+
 // ---- red-black order (the reference's OpenMP EquSolver, placed on a grid) --
 // A cell's colour is the parity of row + col on the grid; a sweep updates the
 // odd cells (the first half of the equation numbering), then the even ones.
@@ -319,8 +486,12 @@ __device__ __forceinline__ void tbp_rb_sweeps(float2 (&P)[R / 2][4], const float
 // float2, i.e. W*R*32*16 bytes per CTA, dynamic) instead of registers,
 // freeing 4R registers per thread for taller regions.
 // RB: red-black sweeps (K is then the apron, 2 x the sweeps per launch).
+// PSEL >= 0 (with !FULL, FP32 Jacobi sweeps): `mask` is the code plane,
+// the sweeps are tbp_sweeps_pin<..., PSEL> and free pixels are not stored;
+// both state buffers must hold the same values at unmasked pixels, which
+// then never change.
 template <int R, int W, int K, bool FULL, typename TS, bool ZS, bool CG = false, bool GS = false,
-          bool RB = false>
+          bool RB = false, int PSEL = -1>
 __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __restrict__ mask,
                                          const float* __restrict__ gc,
                                          const TS* __restrict__ xc, TS* __restrict__ oc,
@@ -359,7 +530,24 @@ __device__ __forceinline__ void tbp_body(const GridGeom& G, const uint8_t* __res
       mk[i + H] = __ldg(reinterpret_cast<const unsigned int*>(mask + pb));
     }
   }
-  if constexpr (RB) {
+  if constexpr (PSEL >= 0 && !FULL) {
+    static_assert(!RB && !GS && std::is_same<TS, float>::value,
+                  "pinned-boundary sweeps: FP32 Jacobi, grad in registers");
+    if (!tbp_sweeps_pin<R, W, PSEL>(P, Gp, mk, ksweeps, lane, w, edge)) return;
+    if (lane >= K / 4 && lane < 32 - K / 4) {
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const int ra = w * R + i, rb = w * R + i + H;  // region rows
+        if (ra >= K && ra < W * R - K)
+          store_kept(oc + base + (long long)i * G.pitch,
+                     make_float4(P[i][0].x, P[i][1].x, P[i][2].x, P[i][3].x), mk[i]);
+        if (rb >= K && rb < W * R - K)
+          store_kept(oc + base + (long long)(i + H) * G.pitch,
+                     make_float4(P[i][0].y, P[i][1].y, P[i][2].y, P[i][3].y), mk[i + H]);
+      }
+    }
+    return;
+  } else if constexpr (RB) {
     static_assert(!GS, "red-black sweeps keep grad in registers");
     tbp_rb_sweeps<R, W, FULL>(P, Gp, mk, ksweeps, lane, w, edge);
   } else {

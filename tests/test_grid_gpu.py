@@ -76,6 +76,73 @@ def test_square800_5000_sweeps_bit_exact(backend):
     np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
 
 
+def test_flow_depths_square800_bit_exact(backend):
+    """The depth-12 flow kernel (104x104 tiles: 8 x 8 of them cover the
+    802-pixel grid, where 96x96 tiles need 9 x 9) after 5000 sweeps, then
+    both depths alternating on one solver (each switch rebuilds the tile
+    tables): states identical to the C oracle's."""
+    mc, t, g, _ = _square800_grid()
+    s = backend.GridSolver(8, 8)
+    s.set_kernel("p16w8k12d")
+    s.reset(mc.size, mc, t, g)
+    img, err = s.step(5000)
+    o = cjacobi.CGrid(mc, t, g)
+    o.sweep(5000)
+    np.testing.assert_array_equal(s.state(), o.x)
+    np.testing.assert_array_equal(img, o.image())
+    np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
+    for kernel, k in (("p16w8k16d", 37), ("p16w8k12d", 50), ("p16w8k16d", 13)):
+        s.set_kernel(kernel)
+        s.step(k)
+        o.sweep(k)
+        assert s.kernel == kernel
+        np.testing.assert_array_equal(s.state(), o.x)
+
+
+@pytest.mark.parametrize("kernel", ["p16w8k16d", "p16w8k12d"])
+@pytest.mark.parametrize("shift", [0, 1, 2, 3])
+def test_flow_pinned_boundary_bodies(backend, kernel, shift):
+    """Regions holding unmasked pixels sweep with selects only at pinned
+    pixels (unmasked, next to a masked one) and leave the other unmasked
+    pixels unstored.  Rectangles shifted by 0..3 columns put their vertical
+    edges in every column group of the lanes (single-group bodies), their
+    horizontal edges make row-selected bodies, a disk the select-everywhere
+    body, and a band on the grid's first columns pins the zero padding next
+    to masked pixels: states and images identical to the C oracle's."""
+    rng = np.random.default_rng(40 + shift)
+    n, m = 300, 430
+    mask = np.zeros((n, m), np.int32)
+    mask[20:280, 10 + shift:400 + shift] = 1
+    mask[0:n, 0:3 + shift] = 1                      # masked pixels on the grid edge
+    yy, xx = np.mgrid[0:n, 0:m]
+    mask[(yy - 150) ** 2 + (xx - 415) ** 2 < 12 ** 2] = 1
+    tgt = rng.uniform(0, 255, (n, m, 3)).astype(np.float32)
+    grad = rng.uniform(-30, 30, (n, m, 3)).astype(np.float32)
+    s = backend.GridSolver(8, 8)
+    s.set_kernel(kernel)
+    s.reset(n * m, mask, tgt, grad)
+    o = cjacobi.CGrid(mask, tgt, grad)
+    for k in (7, 45):
+        img, err = s.step(k)
+        o.sweep(k)
+        np.testing.assert_array_equal(s.state(), o.x)
+        np.testing.assert_array_equal(img, o.image())
+        np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
+
+
+def test_flow_depth12_is_fp32_only(backend):
+    """The depth-12 flow kernel runs FP32 sweeps only: the mixed forms (whose
+    refinement cycles are 64 sweeps of 16-sweep levels) refuse it by name."""
+    from fpie_gb300 import _abi
+
+    d = load_golden("rand24")
+    s = backend.GridSolver(8, 8)
+    s.set_precision("fp16")
+    s.reset(int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
+    with pytest.raises(_abi.FpieArgumentError):
+        s.set_kernel("p16w8k12d")
+
+
 def test_step_continues_and_reset_restarts(backend):
     d = load_golden("rand24")
     args = (int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
@@ -125,7 +192,8 @@ def test_tensor_handoff(backend):
     assert s.launches >= 4  # pack, sweeps, residual/image, finalize
 
 
-KERNELS = ["sweep1", "p16w8k8", "p16w8k16", "p8w16k16", "p8w8k8", "p16w8k16t", "p16w8k16d"]
+KERNELS = ["sweep1", "p16w8k8", "p16w8k16", "p8w16k16", "p8w8k8", "p16w8k16t", "p16w8k16d",
+           "p16w8k12d"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -200,7 +268,7 @@ def _many_items_case():
     return mask, tgt, grad
 
 
-@pytest.mark.parametrize("kernel", ["p16w8k16t", "p16w8k16d"])
+@pytest.mark.parametrize("kernel", ["p16w8k16t", "p16w8k16d", "p16w8k12d"])
 def test_persistent_kernels_many_items_per_cta(backend, kernel):
     """The persistent kernels (TMA prefetch; dependency flow, whose CTAs run
     ahead into the next level where neighbourhoods are ready) on a grid with
@@ -238,7 +306,8 @@ def test_tma_wait_times_out_without_hanging(backend):
     np.testing.assert_array_equal(s.state(), o.x)
 
 
-def test_flow_wait_times_out_without_hanging(backend):
+@pytest.mark.parametrize("kernel", ["p16w8k16d", "p16w8k12d"])
+def test_flow_wait_times_out_without_hanging(backend, kernel):
     """Spin limit 0: a neighbourhood wait of the dependency-flow kernel gives
     up at its first unmet check; the launch stops, the next synchronising
     call raises the timeout, and the solver and GPU stay usable."""
@@ -246,7 +315,7 @@ def test_flow_wait_times_out_without_hanging(backend):
 
     mc, t, g, _ = _square800_grid()
     s = backend.GridSolver(8, 8)
-    s.set_kernel("p16w8k16d")
+    s.set_kernel(kernel)
     s.set_spin_limit(0)
     s.reset(mc.size, mc, t, g)
     with pytest.raises(_abi.FpieTimeoutError):
