@@ -146,11 +146,12 @@ __device__ __forceinline__ bool wait_counters(const FlowArgs& A, const FlowRec& 
   return true;
 }
 
-// One item, out of line: inlined into the item loop, the compiler's register
-// assignment needs several times the register moves per sweep of the same
-// code in the launch-per-tile kernel (measured by instruction counters).
 // One FP32 Jacobi item of a fully masked region (FULL: no selects) or of a
 // region whose unmasked pixels all keep their values by a select (!FULL).
+// Items are out of line: inlined into the item loop, the compiler's
+// register assignment needs several times the register moves per sweep of
+// the same code in the launch-per-tile kernel (measured by instruction
+// counters).
 template <int K, bool FULL>
 __device__ __noinline__ void flow_item(const FlowArgs& A, int tile, int c, int z,
                                        float4 (&edge)[2][2][kW][32], int lane, int w) {
@@ -170,8 +171,8 @@ __device__ __noinline__ void flow_item(const FlowArgs& A, int tile, int c, int z
 // group or in few pair rows, by its body (FlowRec.flag): the pinned-boundary
 // sweeps (code plane, free pixels not stored).  The five bodies share one
 // function (out-of-line bodies of their own measured slower); the select on
-// every unmasked pixel has its own (flow_item), where it runs as fast as
-// alone.
+// every unmasked pixel keeps its own (flow_item), which measured faster than
+// a sixth case here.
 template <int K>
 __device__ __noinline__ void flow_pin_item(const FlowArgs& A, int flag, int tile, int c, int z,
                                            float4 (&edge)[2][2][kW][32], int lane, int w) {
