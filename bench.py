@@ -139,12 +139,13 @@ def measured_peak():
 def kernel_shape(kernel: str, sweeps: int):
     """(sweeps per launch, launches per step, region passes per launch) of a
     grid sweep kernel, from its name: "sweep1"; "p<R>w<W>k<K>[t]" (K sweeps
-    per launch); "p16w8k16d" / "p16w8k12d" / "rb16w8k8d" (dependency flow:
-    the whole step in one launch, a pass per level)."""
+    per launch); "p16w8k16d" / "p16w8k12d" (and their "dp" forms) /
+    "rb16w8k8d" (dependency flow: the whole step in one launch, a pass per
+    level)."""
     if kernel == "sweep1":
         return 1, sweeps, 1
     depth = int(re.search(r"k(\d+)", kernel).group(1))
-    if kernel.endswith("d"):
+    if re.search(r"k\d+dp?$", kernel):
         return sweeps, 1, -(-sweeps // depth)
     return depth, -(-sweeps // depth), 1
 

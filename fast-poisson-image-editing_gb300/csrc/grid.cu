@@ -149,14 +149,23 @@ struct GridSolverImpl : Solver {
   int tma_list_cap = 0;
   int tma_grid = 0;          // persistent CTAs for the current tiling
 
-  // ---- dependency-flow kernel (FP32: variant kFlow or kFlow12; mixed:
-  // mvariant kFlow) ---------------------------------------------------------------
+  // ---- dependency-flow kernel (FP32: variants kFlow, kFlow12, kFlowP,
+  // kFlow12P; mixed: mvariant kFlow) ----------------------------------------------
   // Its tables depend only on the geometry, the mask and the depth.
-  static constexpr int kFlow = -4;    // depth 16 ("p16w8k16d")
-  static constexpr int kFlow12 = -5;  // depth 12 ("p16w8k12d"), FP32 Jacobi only
-  static bool is_flow(int v) { return v == kFlow || v == kFlow12; }
-  // Depth of the flow launches the current settings make.
-  int flow_k() const { return precision == FPIE_FP32 && variant == kFlow12 ? 12 : flow_depth(); }
+  static constexpr int kFlow = -4;     // depth 16 ("p16w8k16d")
+  static constexpr int kFlow12 = -5;   // depth 12 ("p16w8k12d"), FP32 Jacobi only
+  static constexpr int kFlowP = -6;    // depth 16 with pinned-boundary bodies ("p16w8k16dp")
+  static constexpr int kFlow12P = -7;  // depth 12 with them ("p16w8k12dp")
+  static bool is_flow(int v) { return v == kFlow || v == kFlow12 || v == kFlowP || v == kFlow12P; }
+  // Depth of the flow launches the current settings make, and whether they
+  // use the pinned-boundary bodies (FP32 Jacobi only).
+  int flow_k() const {
+    return precision == FPIE_FP32 && (variant == kFlow12 || variant == kFlow12P) ? 12
+                                                                                : flow_depth();
+  }
+  bool flow_pin() const {
+    return precision == FPIE_FP32 && !red_black && (variant == kFlowP || variant == kFlow12P);
+  }
   uint8_t* ft_flags = nullptr;  // tile flags for the flow tiling
   uint8_t* code = nullptr;      // masked / pinned bits per pixel (launch_grid_code)
   int* ft_list = nullptr;       // active-tile list (count + indices)
@@ -191,7 +200,8 @@ struct GridSolverImpl : Solver {
     ensure_flow_tables();
     FPIE_CUDA(cudaMemsetAsync(flow_done, 0, (size_t)ft_tiles * 3 * sizeof(int), stream));
     launch_flow(G, mask, code, g, x[0], x[1], cur, ft_list, flow_rec, flow_done, ft_tiles_x,
-                ft_tiles, iters, d_wait_err, spin_limit, flow_grid, stream, red_black, ft_k);
+                ft_tiles, iters, d_wait_err, spin_limit, flow_grid, stream, red_black, ft_k,
+                flow_pin());
     post_launch(this);
     const int per_level = red_black ? flow_rb_depth() : ft_k;
     const int levels = (iters + per_level - 1) / per_level;
@@ -731,10 +741,12 @@ struct GridSolverImpl : Solver {
     }
     // The dependency-flow kernel runs a whole step per launch; timed on 4
     // chunks per launch so that its start and end (one level each) weigh as
-    // little as in a real step.  Both depths for Jacobi sweeps: which tiling
-    // covers the grid with less work depends on its extents.
-    for (int fv : {kFlow, kFlow12}) {
-      if (fv == kFlow12 && red_black) continue;
+    // little as in a real step.  For Jacobi sweeps both depths (which tiling
+    // covers the grid with less work depends on its extents), each with and
+    // without the pinned-boundary bodies (they pay off on straight mask
+    // edges; the larger kernel runs curved ones slower).
+    for (int fv : {kFlow, kFlow12, kFlowP, kFlow12P}) {
+      if (fv != kFlow && red_black) continue;
       if (iters - used < (kTuneReps + 1) * 4 * kChunk) break;
       select_variant(fv);
       run_flow(4 * kChunk);
@@ -1068,6 +1080,8 @@ struct GridSolverImpl : Solver {
     if (name == "p16w8k16t") v = kTma;
     if (name == "p16w8k16d") v = kFlow;
     if (name == "p16w8k12d") v = kFlow12;
+    if (name == "p16w8k16dp") v = kFlowP;
+    if (name == "p16w8k12dp") v = kFlow12P;
     for (size_t k = 0; k < tb_variants().size(); ++k)
       if (name == tb_variants()[k].name && !tb_variants()[k].red_black) v = (int)k;
     FPIE_REQUIRE(v != -100, FPIE_ERR_ARG, "unknown grid kernel '" + name + "'");
@@ -1082,6 +1096,8 @@ struct GridSolverImpl : Solver {
     if (variant == kFlow && red_black) return std::string(tb_variants()[red_black_variant()].name) + "d";
     if (variant == kFlow) return std::string("p16w8k16d");
     if (variant == kFlow12) return std::string("p16w8k12d");
+    if (variant == kFlowP) return std::string("p16w8k16dp");
+    if (variant == kFlow12P) return std::string("p16w8k12dp");
     return variant < 0 ? std::string("sweep1") : std::string(tb_variants()[variant].name);
   }
 

@@ -32,9 +32,11 @@ size_t flow_rec_bytes();
 // keep its value); the other unmasked pixels are 0.
 void launch_grid_code(const GridGeom& G, const uint8_t* mask, uint8_t* code, cudaStream_t st);
 
-// `sweeps` sweeps on every active tile of the depth-`depth` tiling (Jacobi
-// sweeps read the code plane, launch_grid_code, for regions holding
-// unmasked pixels; the red-black ones the mask), from
+// `sweeps` sweeps on every active tile of the depth-`depth` tiling (with
+// pin_bodies, Jacobi sweeps of regions whose pinned pixels lie in one
+// column group or few pair rows read the code plane, launch_grid_code, and
+// select only there; else every unmasked pixel keeps its value by the
+// mask), from
 // buffer `parity` of {x0, x1}; the result is in buffer
 // (parity + ceil(sweeps / depth)) & 1 (red_black: red-black sweeps at depth
 // 16, ceil(sweeps / 8)).  done (3 ints per active tile) must
@@ -43,8 +45,8 @@ void launch_grid_code(const GridGeom& G, const uint8_t* mask, uint8_t* code, cud
 void launch_flow(const GridGeom& G, const uint8_t* mask, const uint8_t* code, const float* g,
                  float* x0, float* x1, int parity, const int* list, const void* rec, int* done,
                  int tiles_x, int tiles, int sweeps, int* error, long long spin_limit, int ctas,
-                 cudaStream_t st,
-                 bool red_black = false, int depth = 16);
+                 cudaStream_t st, bool red_black = false, int depth = 16,
+                 bool pin_bodies = false);
 
 // The mixed forms (FP16 / BF16 correction, FP32 residual every 64 sweeps)
 // as one launch: the level schedule of the batched kernel (mixed_levels),

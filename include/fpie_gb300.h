@@ -259,16 +259,18 @@ int fpie_grid_solve(fpie_solver* s, double tol, int max_sweeps, int check_every,
  * warps, K sweeps per launch), "p16w8k16d" (the whole step in one
  * cooperative launch, items started by neighbourhood dependencies, levels
  * of 16 sweeps on 96x96 tiles), "p16w8k12d" (the same with levels of 12
- * sweeps on 104x104 tiles; FP32 Jacobi only) or "p16w8k16t" (persistent
- * CTAs prefetching each region by TMA).  Every choice gives bit-identical
- * results. */
+ * sweeps on 104x104 tiles; FP32 Jacobi only), "p16w8k16dp" / "p16w8k12dp"
+ * (the same two with selects only at the unmasked pixels next to masked
+ * ones where a region's mask edge is straight; FP32 Jacobi only) or
+ * "p16w8k16t" (persistent CTAs prefetching each region by TMA).  Every
+ * choice gives bit-identical results. */
 int fpie_grid_set_kernel(fpie_solver* s, const char* name);
 
-/* The dependency-flow kernels ("p16w8k16d", "p16w8k12d") wait for
- * neighbour tiles to finish the previous level, the TMA kernel ("p16w8k16t")
- * for its region copies; each wait gives up after `spins` polls (~64 ns apart), and the
- * step (or fpie_sync) then returns FPIE_ERR_TIMEOUT, leaving the state
- * undefined.  Default 2^26. */
+/* The dependency-flow kernels ("p16w8k16d", "p16w8k12d" and their "dp"
+ * forms) wait for neighbour tiles to finish the previous level, the TMA
+ * kernel ("p16w8k16t") for its region copies; each wait gives up after
+ * `spins` polls (~64 ns apart), and the step (or fpie_sync) then returns
+ * FPIE_ERR_TIMEOUT, leaving the state undefined.  Default 2^26. */
 int fpie_grid_set_spin_limit(fpie_solver* s, long long spins);
 
 /* Writes the current grid sweep kernel's name (NUL-terminated) into buf. */

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = [(1, 1), (1, 7), (7, 1), (2, 2), (3, 3), (2, 300), (300, 3), (5, 129), (131, 130)]
 KERNELS = ["sweep1", "p16w8k8", "p16w8k16", "p8w16k16", "p8w8k8", "p16w8k16t", "p16w8k16d",
-           "p16w8k12d"]
+           "p16w8k12d", "p16w8k16dp", "p16w8k12dp"]
 
 
 def _case(shape, kind, seed):

@@ -137,7 +137,7 @@ def test_grid_placement_equals_gather_components(backend):
     _same_as_gather(backend, d["N"], d["A"], d["X"], d["B"])
 
 
-@pytest.mark.parametrize("kernel", ["p16w8k16", "p16w8k16d", "p16w8k12d", "sweep1"])
+@pytest.mark.parametrize("kernel", ["p16w8k16", "p16w8k16d", "p16w8k12d", "p16w8k12dp", "sweep1"])
 def test_grid_placement_pinned_kernels(backend, kernel):
     d = _two_disks_system()
     s = backend.EquSolver(256)

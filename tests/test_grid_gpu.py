@@ -91,7 +91,8 @@ def test_flow_depths_square800_bit_exact(backend):
     np.testing.assert_array_equal(s.state(), o.x)
     np.testing.assert_array_equal(img, o.image())
     np.testing.assert_allclose(err, o.err64(), rtol=1e-5)
-    for kernel, k in (("p16w8k16d", 37), ("p16w8k12d", 50), ("p16w8k16d", 13)):
+    for kernel, k in (("p16w8k16d", 37), ("p16w8k12dp", 50), ("p16w8k16dp", 21),
+                      ("p16w8k12d", 13)):
         s.set_kernel(kernel)
         s.step(k)
         o.sweep(k)
@@ -99,7 +100,7 @@ def test_flow_depths_square800_bit_exact(backend):
         np.testing.assert_array_equal(s.state(), o.x)
 
 
-@pytest.mark.parametrize("kernel", ["p16w8k16d", "p16w8k12d"])
+@pytest.mark.parametrize("kernel", ["p16w8k16dp", "p16w8k12dp"])
 @pytest.mark.parametrize("shift", [0, 1, 2, 3])
 def test_flow_pinned_boundary_bodies(backend, kernel, shift):
     """Regions holding unmasked pixels sweep with selects only at pinned
@@ -131,16 +132,18 @@ def test_flow_pinned_boundary_bodies(backend, kernel, shift):
 
 
 def test_flow_depth12_is_fp32_only(backend):
-    """The depth-12 flow kernel runs FP32 sweeps only: the mixed forms (whose
-    refinement cycles are 64 sweeps of 16-sweep levels) refuse it by name."""
+    """The depth-12 and pinned-boundary flow kernels run FP32 sweeps only:
+    the mixed forms (whose refinement cycles are 64 sweeps of 16-sweep
+    levels) refuse them by name."""
     from fpie_gb300 import _abi
 
     d = load_golden("rand24")
     s = backend.GridSolver(8, 8)
     s.set_precision("fp16")
     s.reset(int(d["grid_n"]), d["grid_mask"], d["grid_tgt"], d["grid_grad"])
-    with pytest.raises(_abi.FpieArgumentError):
-        s.set_kernel("p16w8k12d")
+    for name in ("p16w8k12d", "p16w8k12dp", "p16w8k16dp"):
+        with pytest.raises(_abi.FpieArgumentError):
+            s.set_kernel(name)
 
 
 def test_step_continues_and_reset_restarts(backend):
@@ -193,7 +196,7 @@ def test_tensor_handoff(backend):
 
 
 KERNELS = ["sweep1", "p16w8k8", "p16w8k16", "p8w16k16", "p8w8k8", "p16w8k16t", "p16w8k16d",
-           "p16w8k12d"]
+           "p16w8k12d", "p16w8k16dp", "p16w8k12dp"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -268,7 +271,7 @@ def _many_items_case():
     return mask, tgt, grad
 
 
-@pytest.mark.parametrize("kernel", ["p16w8k16t", "p16w8k16d", "p16w8k12d"])
+@pytest.mark.parametrize("kernel", ["p16w8k16t", "p16w8k16d", "p16w8k12d", "p16w8k12dp"])
 def test_persistent_kernels_many_items_per_cta(backend, kernel):
     """The persistent kernels (TMA prefetch; dependency flow, whose CTAs run
     ahead into the next level where neighbourhoods are ready) on a grid with
