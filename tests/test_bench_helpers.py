@@ -58,3 +58,17 @@ def test_median_step_time_resets_before_each_step():
     calls = []
     s = bench._median_step_s(lambda: calls.append("r"), lambda k: calls.append(k), 7, reps=3)
     assert calls == ["r", 7, "r", 7, "r", 7] and s >= 0.0
+
+
+def test_kernel_shape_and_apron_of_every_grid_kernel_name():
+    """Sweeps per launch, launches per step and region passes per launch,
+    and the apron factor, from the kernel names the solver reports."""
+    assert bench.kernel_shape("sweep1", 5000) == (1, 5000, 1)
+    assert bench.kernel_shape("p16w8k16", 5000) == (16, 313, 1)
+    for name, depth in (("p16w8k16d", 16), ("p16w8k12d", 12), ("p16w8k16dp", 16),
+                        ("p16w8k12dp", 12), ("rb16w8k8d", 8)):
+        assert bench.kernel_shape(name, 5000) == (5000, 1, -(-5000 // depth)), name
+    assert abs(bench.apron_factor("p16w8k16d") - 128 * 128 / (96 * 96)) < 1e-12
+    assert abs(bench.apron_factor("p16w8k12dp") - 128 * 128 / (104 * 104)) < 1e-12
+    assert abs(bench.apron_factor("rb16w8k8d") - 128 * 128 / (96 * 96)) < 1e-12
+    assert bench.apron_factor("sweep1") == 1.0
