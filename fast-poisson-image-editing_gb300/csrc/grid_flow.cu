@@ -97,7 +97,16 @@ struct FlowArgs {
   int tiles_x, sweeps, parity;
   long long spin_limit;
   int red_black;         // red-black sweeps: kK / 2 per level, same tiles and apron
+  int smem_recs;         // the records are copied to shared memory first
 };
+
+// Records of at most this many active tiles (30 KB; with the 16 KB of edge
+// rows the kernel stays under the default 48 KB of shared memory, so L1
+// keeps its size) are copied to shared memory at the start of a launch.
+// Thread 0 reads the next item's record after the current item and only
+// then can load its neighbourhood counters: from L2 that is two round trips
+// before the release barrier, which holds back this item's release.
+constexpr int kFlowRecsSmem = 640;
 
 __device__ __forceinline__ FlowRec load_rec(const FlowRec* r) {
   const int4* q = reinterpret_cast<const int4*>(r);
@@ -308,8 +317,17 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
   static_assert(K == kK || !MIXED, "the mixed forms' cycles are 64 sweeps of kK-sweep levels");
   __shared__ float4 edge[2][2][kW][32];
   __shared__ int s_stop, s_tile, s_flag;
+  extern __shared__ __align__(16) unsigned char flow_dyn[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int per = 3 * A.list[-1];
+  const FlowRec* recs = A.rec;
+  if (A.smem_recs) {  // uniform per launch
+    int4* dst = reinterpret_cast<int4*>(flow_dyn);
+    const int4* src = reinterpret_cast<const int4*>(A.rec);
+    for (int k = threadIdx.x; k < per; k += blockDim.x) dst[k] = src[k];  // 3 int4 per record
+    __syncthreads();
+    recs = reinterpret_cast<const FlowRec*>(flow_dyn);
+  }
   const int per_level = A.red_black ? K / 2 : K;
   const int levels = MIXED ? mixed_levels(A.sweeps, K) : (A.sweeps + per_level - 1) / per_level;
   const long long total = (long long)levels * per;
@@ -317,7 +335,7 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
   int v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (threadIdx.x == 0 && blockIdx.x < total) {
     const int r = (int)blockIdx.x % per;
-    R = load_rec(A.rec + r / 3);
+    R = load_rec(recs + r / 3);
     load_counters(A, R, r % 3, v);
   }
   for (long long idx = blockIdx.x; idx < total; idx += gridDim.x) {
@@ -365,7 +383,7 @@ __global__ void __launch_bounds__(kW * 32, 1) grid_flow_kernel(FlowArgs A) {
     const long long next = idx + gridDim.x;
     if (threadIdx.x == 0 && next < total) {
       const int rn = (int)(next % per);
-      R = load_rec(A.rec + rn / 3);
+      R = load_rec(recs + rn / 3);
       load_counters(A, R, rn % 3, v);
     }
     // Release: the CTA barrier orders every thread's writes before the
@@ -471,6 +489,12 @@ int flow_tile_w(int depth) { return depth == 12 ? FlowTile<12>::W : FlowTile<kK>
 int flow_depth() { return kK; }
 int flow_rb_depth() { return kK / 2; }
 
+// Dynamic shared memory of a launch over `tiles` tiles (at most that many
+// active): every record when they fit, else none.
+static size_t flow_rec_smem(int tiles) {
+  return tiles <= kFlowRecsSmem ? sizeof(FlowRec) * (size_t)tiles : 0;
+}
+
 int flow_ctas() {
   // Occupancy queries cost tens of microseconds; the answer is fixed per
   // device, and every reset rebuilds the flow tables.
@@ -488,7 +512,8 @@ int flow_ctas() {
                        (const void*)grid_flow_kernel<__half, kK>,
                        (const void*)grid_flow_kernel<__nv_bfloat16, kK>};
   for (const void* k : ks) {
-    FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kW * 32, 0));
+    FPIE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kW * 32,
+                                                            sizeof(FlowRec) * kFlowRecsSmem));
     m = std::min(m, per_sm);
   }
   FPIE_REQUIRE(m >= 1, FPIE_ERR_CUDA, "the flow sweep kernel does not fit on an SM");
@@ -525,7 +550,7 @@ void launch_flow(const GridGeom& G, const uint8_t* mask, const uint8_t* code, co
                "flow sweep kernel: bad tiling");
   FlowArgs a{G, mask, code, g, {x0, x1}, {nullptr, nullptr}, nullptr, list + 1,
              static_cast<const FlowRec*>(rec), done, error, tiles_x, sweeps, parity & 1,
-             spin_limit, red_black ? 1 : 0};
+             spin_limit, red_black ? 1 : 0, flow_rec_smem(tiles) > 0 ? 1 : 0};
   void* args[] = {&a};
   FPIE_REQUIRE(!pin_bodies || !red_black, FPIE_ERR_ARG,
                "flow sweep kernel: pinned-boundary bodies are for Jacobi sweeps");
@@ -533,7 +558,8 @@ void launch_flow(const GridGeom& G, const uint8_t* mask, const uint8_t* code, co
                                             : (const void*)grid_flow_kernel<float, 12>)
                               : (pin_bodies ? (const void*)grid_flow_kernel<float, kK, true>
                                             : (const void*)grid_flow_kernel<float, kK>);
-  FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, 0, st));
+  FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, flow_rec_smem(tiles),
+                                        st));
 }
 
 void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, float* x0, float* x1,
@@ -544,11 +570,12 @@ void launch_flow_mixed(const GridGeom& G, const uint8_t* mask, const float* g, f
   FPIE_REQUIRE(tiles_x >= 1 && tiles % tiles_x == 0 && ctas >= 1, FPIE_ERR_STATE,
                "flow sweep kernel: bad tiling");
   FlowArgs a{G, mask, nullptr, g, {x0, x1}, {e0, e1}, r, list + 1, static_cast<const FlowRec*>(rec), done,
-             error, tiles_x, sweeps, parity & 1, spin_limit, 0};
+             error, tiles_x, sweeps, parity & 1, spin_limit, 0, flow_rec_smem(tiles) > 0 ? 1 : 0};
   void* args[] = {&a};
   const void* k = bf16 ? (const void*)grid_flow_kernel<__nv_bfloat16, kK>
                        : (const void*)grid_flow_kernel<__half, kK>;
-  FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, 0, st));
+  FPIE_CUDA(cudaLaunchCooperativeKernel(k, dim3(ctas), dim3(kW * 32), args, flow_rec_smem(tiles),
+                                        st));
 }
 
 int flow_mixed_flips(int sweeps) { return (sweeps + 63) / 64; }
